@@ -1,0 +1,148 @@
+/*
+ * rgf.h -- C ABI of the GB300-native RGF solver (sm_103a).
+ *
+ * Solves with a symmetric positive-definite block-tridiagonal-arrowhead
+ * matrix of size n = ns*nt + nd, given as its lower triangle in CSC form
+ * with size_t indices (ia: n+1 column pointers, ja: row indices, row >= col,
+ * a: values).  This is the input of the reference class
+ *     RGF<double>::RGF(size_t *ia, size_t *ja, double *a,
+ *                      size_t ns, size_t nt, size_t nd)      (RGF.H:84-146)
+ *
+ * Every entry point returns an int status (enum rgf_status).  Host pointers
+ * are plain host memory (pageable or pinned); device memory is owned by the
+ * handle.  One call at a time per handle; different handles may be used from
+ * different host threads.  All computation runs on the GPU: there is no CPU
+ * fallback, and a missing or unusable device is reported as RGF_ECUDA.
+ */
+#ifndef RGF_GB300_RGF_H
+#define RGF_GB300_RGF_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum rgf_status {
+  RGF_OK = 0,
+  RGF_EINVAL = 1,    /* bad argument or CSC outside the block pattern        */
+  RGF_ENOMEM = 2,    /* device allocation failed                              */
+  RGF_ENOTSPD = 3,   /* non-positive pivot: matrix not positive definite      */
+  RGF_ECUDA = 4,     /* CUDA runtime error / no usable device                 */
+  RGF_ETIMEOUT = 5,  /* a bounded device-side wait gave up                    */
+  RGF_ENOTSUP = 6    /* option not supported by this build                    */
+};
+
+enum rgf_precision {
+  RGF_PREC_FP64 = 0,   /* every operation in FP64                             */
+  RGF_PREC_SPLIT = 1   /* bulk GEMMs as bf16 slice products on tcgen05 tensor
+                          cores (Ozaki scheme), FP64 elsewhere                */
+};
+
+enum rgf_selinv_mode {
+  RGF_SELINV_EXACT = 0,  /* exact block selected inversion                    */
+  RGF_SELINV_COMPAT = 1  /* the reference's recursion (RGF.H:422-506), which
+                            omits the arrowhead cross terms when nd > 0       */
+};
+
+typedef struct rgf_opts {
+  int precision;    /* enum rgf_precision (default RGF_PREC_FP64)             */
+  int slices;       /* split precision: slices per operand, 0 = default       */
+  int selinv_mode;  /* enum rgf_selinv_mode (default RGF_SELINV_EXACT)        */
+  int device;       /* CUDA device ordinal, -1 = the current device           */
+  int use_graphs;   /* 1 = replay each stage as a captured CUDA graph         */
+  int reserved[11];
+} rgf_opts;
+
+typedef struct rgf_handle rgf_handle;
+
+/* Sizes of one instance (RGF.H:94-95). */
+typedef struct rgf_info_t {
+  size_t n;          /* ns*nt + nd                                           */
+  size_t nnz;        /* stored lower non-zeros (ia[n])                       */
+  size_t mf_size;    /* doubles in the block-column factor layout MF         */
+  size_t device_bytes; /* device memory held by the handle                   */
+  int not_spd_column;  /* first column with a non-positive pivot, or -1      */
+  int reserved0;
+  long long kernels_launched; /* GPU kernels launched by this handle so far   */
+  int reserved[4];
+} rgf_info_t;
+
+/* Human-readable name of a status code. */
+const char* rgf_status_string(int status);
+
+/* Fill *opts with defaults. */
+int rgf_default_opts(rgf_opts* opts);
+
+/* Replaces RGF<double>::RGF (RGF.H:84-146).  Validates the CSC against the
+ * block-tridiagonal-arrowhead pattern and copies it to the device, so the
+ * caller's arrays may be freed after the call.  opts may be NULL. */
+int rgf_create(const size_t* ia, const size_t* ja, const double* a,
+               size_t ns, size_t nt, size_t nd,
+               const rgf_opts* opts, rgf_handle** out);
+
+/* Replaces RGF<double>::~RGF (RGF.H:150-170). */
+int rgf_destroy(rgf_handle* h);
+
+/* Replaces RGF<double>::factorize (RGF.H:510-546, FirstStageFactor
+ * RGF.H:233-340).  The factor stays resident on the device. */
+int rgf_factorize(rgf_handle* h);
+
+/* Replaces RGF<double>::logDet (RGF.H:616-627): 2*sum(log L_kk).
+ * Factorizes first if needed. */
+int rgf_logdet(rgf_handle* h, double* logdet);
+
+/* Replaces RGF<double>::solve(x, b, nrhs) (RGF.H:559-578,
+ * SecondStageSolve RGF.H:344-418).  b and x are n x nrhs column-major
+ * (ld = n) host arrays; x may equal b (RGF.H:550-554).  Factorizes first if
+ * needed. */
+int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs);
+
+/* Replaces RGF<double>::RGFdiag (RGF.H:582-612, ThirdStageRGF
+ * RGF.H:422-506): diag(A^{-1}) into the host array diag[n].  Unlike the
+ * reference, the factor is not invalidated. */
+int rgf_diag(rgf_handle* h, double* diag);
+
+/* Replaces RGF<double>::residualNorm (RGF.H:631-655): ||b - A x||_2 of the
+ * first right-hand side, computed on the device from the stored CSC. */
+int rgf_residual_norm(rgf_handle* h, const double* x, const double* b, double* norm);
+
+/* Replaces RGF<double>::residualNormNormalized (RGF.H:659-663). */
+int rgf_residual_norm_normalized(rgf_handle* h, const double* x, const double* b,
+                                 double* norm);
+
+/* Copy the factor, in the reference's block-column layout MF (RGF.H:95,
+ * 114-138), to the host array mf[mf_size].  Only the lower triangles of the
+ * diagonal blocks are defined; the strict upper triangles are zero. */
+int rgf_export_factor(rgf_handle* h, double* mf);
+
+/* Copy the selected inverse to the host in the MF layout: Sigma_ii (full
+ * block), Sigma_{i+1,i}, Sigma_{d,i} and Sigma_dd in the positions of
+ * L_ii, L_{i+1,i}, C_i and L_dd.  Runs the selected inversion if needed.
+ * Only RGF_SELINV_EXACT defines the off-diagonal blocks. */
+int rgf_export_selinv(rgf_handle* h, double* ms);
+
+/* Sizes and last-failure details. */
+int rgf_get_info(rgf_handle* h, rgf_info_t* info);
+
+/* Device-resident results (for callers that keep data on the GPU):
+ * the selected-inverse diagonal, n doubles owned by the handle. */
+int rgf_diag_device(rgf_handle* h, const double** d_diag);
+
+/* The CUDA stream (cudaStream_t) all work of this handle is issued on. */
+int rgf_get_stream(rgf_handle* h, void** stream);
+
+/* Kernel timer: while enabled, every launch of the bulk GEMM kernels of this
+ * handle is bracketed by CUDA events on the handle's stream; *ms receives the
+ * summed device time, *launches their number and *flops their algorithmic
+ * FP64-equivalent flops since the last reset.  Stages run without CUDA graphs
+ * while the timer is enabled. */
+int rgf_kernel_timer_enable(rgf_handle* h, int enable);
+int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launches,
+                          double* flops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RGF_GB300_RGF_H */

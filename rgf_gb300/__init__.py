@@ -1,0 +1,250 @@
+"""rgf_gb300 -- GB300-native drop-in for the reference ``RGF<double>`` solver.
+
+``RGF`` mirrors the public surface of the reference class (``RGF.H:11-80``):
+construct with ``(ia, ja, a, ns, nt, nd)`` on the lower triangle of a
+symmetric positive-definite block-tridiagonal-arrowhead matrix in CSC form,
+then ``factorize``, ``logDet``, ``solve`` and ``RGFdiag``.  Every call goes
+through the C ABI of ``librgf_gb300.so`` (``include/rgf.h``); all arithmetic
+runs in hand-written sm_103a kernels.  There is no CPU fallback: without the
+built library or a usable GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["RGF", "RGFError", "load_library", "library_path", "STATUS"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+STATUS = {0: "RGF_OK", 1: "RGF_EINVAL", 2: "RGF_ENOMEM", 3: "RGF_ENOTSPD",
+          4: "RGF_ECUDA", 5: "RGF_ETIMEOUT", 6: "RGF_ENOTSUP"}
+PRECISION = {"fp64": 0, "split": 1}
+SELINV = {"exact": 0, "compat": 1}
+
+
+class RGFError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, status: int, what: str):
+        self.status = status
+        msg = _LIB.rgf_status_string(status).decode() if _LIB is not None else STATUS.get(status)
+        super().__init__(f"{what}: {msg}")
+
+
+class _Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("slices", C.c_int), ("selinv_mode", C.c_int),
+                ("device", C.c_int), ("use_graphs", C.c_int), ("reserved", C.c_int * 11)]
+
+
+class _Info(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("nnz", C.c_size_t), ("mf_size", C.c_size_t),
+                ("device_bytes", C.c_size_t), ("not_spd_column", C.c_int),
+                ("reserved0", C.c_int), ("kernels_launched", C.c_longlong),
+                ("reserved", C.c_int * 4)]
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "librgf_gb300.so")
+
+
+_SIGS = {
+    "rgf_status_string": (C.c_char_p, [C.c_int]),
+    "rgf_default_opts": (C.c_int, [C.POINTER(_Opts)]),
+    "rgf_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
+                             C.c_size_t, C.POINTER(_Opts), C.POINTER(C.c_void_p)]),
+    "rgf_destroy": (C.c_int, [C.c_void_p]),
+    "rgf_factorize": (C.c_int, [C.c_void_p]),
+    "rgf_logdet": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "rgf_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "rgf_diag": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgf_residual_norm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "rgf_residual_norm_normalized": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.POINTER(C.c_double)]),
+    "rgf_export_factor": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgf_export_selinv": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgf_get_info": (C.c_int, [C.c_void_p, C.POINTER(_Info)]),
+    "rgf_diag_device": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rgf_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rgf_kernel_timer_enable": (C.c_int, [C.c_void_p, C.c_int]),
+    "rgf_kernel_timer_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+}
+
+
+def load_library(path: str | None = None):
+    """Load librgf_gb300.so (built by ``rgf_gb300.build``); raise if absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or library_path()
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is not built: run `python -m rgf_gb300.build` "
+                           "(requires nvcc); there is no CPU fallback")
+    lib = C.CDLL(p)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != 0:
+        raise RGFError(status, what)
+
+
+def _ptr(arr: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(arr.ctypes.data)
+
+
+class RGF:
+    """Drop-in for the reference class ``RGF<double>`` (``RGF.H:11-80``).
+
+    ``ia``/``ja`` are the column pointers and row indices (``size_t``) and
+    ``a`` the values of the matrix's lower triangle in CSC form.  Unlike the
+    reference, the arrays are copied to the device at construction.
+    """
+
+    def __init__(self, ia, ja, a, ns: int, nt: int, nd: int, precision: str = "fp64",
+                 slices: int = 0, selinv: str = "exact", device: int = -1,
+                 use_graphs: bool = True):
+        lib = load_library()
+        self._lib = lib
+        self._h = C.c_void_p()
+        self.ns, self.nt, self.nd = int(ns), int(nt), int(nd)
+        self.n = self.ns * self.nt + self.nd
+        self._ia = np.ascontiguousarray(ia, dtype=np.uint64)
+        self._ja = np.ascontiguousarray(ja, dtype=np.uint64)
+        self._a = np.ascontiguousarray(a, dtype=np.float64)
+        if self._ia.size != self.n + 1:
+            raise ValueError(f"ia must have n+1 = {self.n + 1} entries")
+        nnz = int(self._ia[-1])
+        if self._ja.size < nnz or self._a.size < nnz:
+            raise ValueError("ja/a shorter than ia[n]")
+        o = _Opts()
+        lib.rgf_default_opts(C.byref(o))
+        o.precision = PRECISION[precision]
+        o.slices = int(slices)
+        o.selinv_mode = SELINV[selinv]
+        o.device = int(device)
+        o.use_graphs = 1 if use_graphs else 0
+        _check(lib.rgf_create(_ptr(self._ia), _ptr(self._ja), _ptr(self._a), self.ns, self.nt,
+                              self.nd, C.byref(o), C.byref(self._h)), "rgf_create")
+
+    # -- reference methods ----------------------------------------------------
+    def factorize(self) -> None:
+        """RGF.H:510-546."""
+        _check(self._lib.rgf_factorize(self._h), "rgf_factorize")
+
+    def logDet(self) -> float:
+        """RGF.H:616-627."""
+        out = C.c_double()
+        _check(self._lib.rgf_logdet(self._h, C.byref(out)), "rgf_logdet")
+        return out.value
+
+    def solve(self, x, b=None, nrhs: int | None = None):
+        """``solve(b, nrhs)`` in place (RGF.H:550-554) or ``solve(x, b, nrhs)``
+        (RGF.H:559-578).  Arrays are n x nrhs column-major (ld = n); returns x."""
+        if b is None:
+            b = x
+        b = np.asarray(b, dtype=np.float64)
+        if nrhs is None:
+            nrhs = 1 if b.ndim == 1 else b.shape[1]
+        bf = np.asfortranarray(b.reshape(self.n, nrhs) if b.ndim == 1 else b)
+        out = np.empty((self.n, nrhs), dtype=np.float64, order="F")
+        _check(self._lib.rgf_solve(self._h, _ptr(out), _ptr(bf), int(nrhs)), "rgf_solve")
+        if isinstance(x, np.ndarray) and x.size == out.size:
+            if x.ndim == 1:
+                x[:] = out.ravel(order="F")
+            else:
+                x[...] = out.reshape(x.shape, order="F")
+        return out[:, 0] if b.ndim == 1 else out
+
+    def RGFdiag(self, diag=None) -> np.ndarray:
+        """RGF.H:582-612: diag(A^{-1})."""
+        out = np.empty(self.n, dtype=np.float64)
+        _check(self._lib.rgf_diag(self._h, _ptr(out)), "rgf_diag")
+        if diag is not None:
+            diag[:] = out
+        return out
+
+    def residualNorm(self, x, b) -> float:
+        """RGF.H:631-655 (first right-hand side)."""
+        xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
+        bb = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
+        out = C.c_double()
+        _check(self._lib.rgf_residual_norm(self._h, _ptr(xx), _ptr(bb), C.byref(out)),
+               "rgf_residual_norm")
+        return out.value
+
+    def residualNormNormalized(self, x, b) -> float:
+        """RGF.H:659-663."""
+        xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
+        bb = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
+        out = C.c_double()
+        _check(self._lib.rgf_residual_norm_normalized(self._h, _ptr(xx), _ptr(bb), C.byref(out)),
+               "rgf_residual_norm_normalized")
+        return out.value
+
+    # -- extensions -------------------------------------------------------------
+    def export_factor(self) -> np.ndarray:
+        """The factor in the reference's MF layout (lower triangles defined)."""
+        info = self.info()
+        out = np.empty(info["mf_size"], dtype=np.float64)
+        _check(self._lib.rgf_export_factor(self._h, _ptr(out)), "rgf_export_factor")
+        return out
+
+    def export_selinv(self) -> np.ndarray:
+        """Selected inverse blocks in the MF layout."""
+        info = self.info()
+        out = np.empty(info["mf_size"], dtype=np.float64)
+        _check(self._lib.rgf_export_selinv(self._h, _ptr(out)), "rgf_export_selinv")
+        return out
+
+    def info(self) -> dict:
+        i = _Info()
+        _check(self._lib.rgf_get_info(self._h, C.byref(i)), "rgf_get_info")
+        return {"n": i.n, "nnz": i.nnz, "mf_size": i.mf_size, "device_bytes": i.device_bytes,
+                "not_spd_column": i.not_spd_column, "kernels_launched": i.kernels_launched}
+
+    def diag_device_ptr(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.rgf_diag_device(self._h, C.byref(p)), "rgf_diag_device")
+        return p.value
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.rgf_get_stream(self._h, C.byref(p)), "rgf_get_stream")
+        return p.value or 0
+
+    def kernel_timer(self, enable: bool) -> None:
+        _check(self._lib.rgf_kernel_timer_enable(self._h, 1 if enable else 0), "timer")
+
+    def kernel_timer_read(self, reset: bool = True) -> dict:
+        ms, n, fl = C.c_double(), C.c_longlong(), C.c_double()
+        _check(self._lib.rgf_kernel_timer_read(self._h, 1 if reset else 0, C.byref(ms),
+                                               C.byref(n), C.byref(fl)), "timer")
+        return {"ms": ms.value, "launches": n.value, "flops": fl.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.rgf_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

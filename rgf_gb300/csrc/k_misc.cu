@@ -1,0 +1,255 @@
+// Memory-bound kernels of the RGF recursion: CSC ingest into the block
+// layout, reductions, diagonal extraction, residual SpMV and small helpers.
+#include <cmath>
+#include <cstdint>
+
+#include "rgf_internal.h"
+
+namespace rgf {
+
+// Block-column layout (the reference's MF, RGF.H:95, 114-138):
+// block column i < nt-1 is (2ns+nd) x ns = [L_ii; L_{i+1,i}; C_i],
+// block column nt-1 is (ns+nd) x ns = [L_ii; C_i], the corner is nd x nd.
+__host__ __device__ inline long long col_offset_d(long long ns, long long nt, long long nd,
+                                                  long long i) {
+  if (i < nt) return i * ns * (2 * ns + nd);
+  return (nt - 1) * ns * (2 * ns + nd) + ns * (ns + nd);
+}
+__host__ __device__ inline long long lda_d(long long ns, long long nt, long long nd, long long i) {
+  if (i < nt - 1) return 2 * ns + nd;
+  if (i < nt) return ns + nd;
+  return nd;
+}
+__host__ __device__ inline long long dense_row_d(long long ns, long long nt, long long i) {
+  if (i < nt - 1) return 2 * ns;
+  if (i == nt - 1) return ns;
+  return 0;
+}
+
+long long mf_col_offset(const BtaShape& sh, long long i) { return col_offset_d(sh.ns, sh.nt, sh.nd, i); }
+long long mf_lda(const BtaShape& sh, long long i) { return lda_d(sh.ns, sh.nt, sh.nd, i); }
+long long mf_dense_row(const BtaShape& sh, long long i) { return dense_row_d(sh.ns, sh.nt, i); }
+
+namespace {
+
+// One warp per CSC column: the column's block column and panel offset are
+// computed once, then every entry maps to a row of that panel.  Follows the
+// mapping of the reference's getPos (CWC_utility.cu:998-1029) without its
+// per-entry linear column search (CWC_utility.cu:1093-1095).
+__global__ void ingest_kernel(BtaShape sh, const size_t* __restrict__ ia,
+                              const size_t* __restrict__ ja, const double* __restrict__ a,
+                              double* __restrict__ MF, DevStatus* st) {
+  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= sh.n) return;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd, n = sh.n;
+  const long long ib = c < ns * nt ? c / ns : nt;
+  const long long jc = ib < nt ? c - ib * ns : c - nt * ns;
+  const long long off = col_offset_d(ns, nt, nd, ib);
+  const long long lda = lda_d(ns, nt, nd, ib);
+  const long long ro = dense_row_d(ns, nt, ib);
+  const size_t e0 = ia[c], e1 = ia[c + 1];
+  bool bad = false;
+  for (size_t e = e0 + lane; e < e1; e += 32) {
+    const long long r = (long long)ja[e];
+    bool ok = r >= c && r < n;
+    long long row = 0;
+    if (ok) {
+      const long long rb = r < ns * nt ? r / ns : nt;
+      if (rb == ib) row = (ib < nt) ? r - ib * ns : r - nt * ns;
+      else if (rb == ib + 1 && rb < nt) row = r - ib * ns;
+      else if (rb == nt) row = ro + (r - nt * ns);
+      else ok = false;
+    }
+    if (ok) MF[off + jc * lda + row] = a[e];
+    else bad = true;
+  }
+  if (bad) atomicOr(&st->bad_input, 1);
+}
+
+__global__ void logdet_reduce_kernel(const double* parts, int nparts, double* out) {
+  const int lane = threadIdx.x;
+  double s = 0.0;
+  for (int i = lane; i < nparts; i += 32) s += parts[i];
+  __shared__ double ws[32];
+  ws[lane] = s;
+  __syncwarp();
+  if (lane == 0) {
+    double t = 0.0;
+    for (int i = 0; i < 32; ++i) t += ws[i];
+    *out = 2.0 * t;
+  }
+}
+
+__global__ void extract_diag_kernel(BtaShape sh, const double* MS, double* diag) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sh.n) return;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
+  long long pos;
+  if (k < ns * nt) {
+    const long long i = k / ns, j = k - i * ns;
+    pos = col_offset_d(ns, nt, nd, i) + j * (lda_d(ns, nt, nd, i) + 1);
+  } else {
+    const long long j = k - ns * nt;
+    pos = col_offset_d(ns, nt, nd, nt) + j * (nd + 1);
+  }
+  diag[k] = MS[pos];
+}
+
+__global__ void set_identity_kernel(double* X, long long ld, int m, long long stride) {
+  X += (long long)blockIdx.z * stride;
+  const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
+  if (r < m && c < m) X[r + (long long)c * ld] = (r == c) ? 1.0 : 0.0;
+}
+
+__global__ void copy_kernel(const double* X, long long ldx, double* Y, long long ldy, int m,
+                            int n, long long sX, long long sY) {
+  X += (long long)blockIdx.z * sX;
+  Y += (long long)blockIdx.z * sY;
+  const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
+  if (r < m && c < n) Y[r + (long long)c * ldy] = X[r + (long long)c * ldx];
+}
+
+__global__ void zero_upper_kernel(double* X, long long ld, int m, long long stride) {
+  X += (long long)blockIdx.z * stride;
+  const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
+  if (r < m && c < m && r < c) X[r + (long long)c * ld] = 0.0;
+}
+
+// y = A x with A symmetric, stored as its lower CSC: column c contributes
+// a_rc x_c to y_r (scatter) and, off the diagonal, a_rc x_r to y_c (gather).
+__global__ void sym_spmv_kernel(long long n, const size_t* __restrict__ ia,
+                                const size_t* __restrict__ ja, const double* __restrict__ a,
+                                const double* __restrict__ x, double* y) {
+  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= n) return;
+  const double xc = x[c];
+  double g = 0.0;
+  for (size_t e = ia[c] + lane; e < ia[c + 1]; e += 32) {
+    const long long r = (long long)ja[e];
+    const double v = a[e];
+    atomicAdd(&y[r], v * xc);
+    if (r != c) g += v * x[r];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+  if (lane == 0 && g != 0.0) atomicAdd(&y[c], g);
+}
+
+__global__ void residual_norm_kernel(long long n, const double* b, const double* y, double* out) {
+  __shared__ double s1[1024], s2[1024];
+  double r2 = 0.0, b2 = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = b[i] - y[i];
+    r2 += r * r;
+    b2 += b[i] * b[i];
+  }
+  s1[threadIdx.x] = r2;
+  s2[threadIdx.x] = b2;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      s1[threadIdx.x] += s1[threadIdx.x + w];
+      s2[threadIdx.x] += s2[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sqrt(s1[0]);
+    out[1] = sqrt(s2[0]);
+  }
+}
+
+// partial[i][q][dd] = sum_j C_i(dd, j) * rhs_i(j, q): one CTA per block
+// column i, one warp per (dd, q) pair, fixed-order warp reduction.
+__global__ void arrow_gemv_kernel(BtaShape sh, const double* MF, const double* rhs, long long ldr,
+                                  int nrhs, double* partial) {
+  const long long i = blockIdx.x;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
+  const double* Cb = MF + col_offset_d(ns, nt, nd, i) + dense_row_d(ns, nt, i);
+  const long long lda = lda_d(ns, nt, nd, i);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int p = warp; p < nd * nrhs; p += nw) {
+    const int dd = p % nd, q = p / nd;
+    const double* R = rhs + i * ns + (long long)q * ldr;
+    double s = 0.0;
+    for (long long j = lane; j < ns; j += 32) s += Cb[dd + j * lda] * R[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) partial[(i * nrhs + q) * nd + dd] = s;
+  }
+}
+
+__global__ void arrow_reduce_kernel(BtaShape sh, const double* partial, int nrhs, double* rhs,
+                                    long long ldr) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nd = sh.nd;
+  if (p >= nd * nrhs) return;
+  const int dd = p % nd, q = p / nd;
+  double s = 0.0;
+  for (long long i = 0; i < sh.nt; ++i) s += partial[(i * nrhs + q) * nd + dd];
+  rhs[sh.nt * sh.ns + dd + (long long)q * ldr] -= s;
+}
+
+}  // namespace
+
+void launch_ingest(const BtaShape& sh, const size_t* ia, const size_t* ja, const double* a,
+                   double* MF, DevStatus* st, cudaStream_t s) {
+  const long long threads = sh.n * 32;
+  const int bs = 256;
+  ingest_kernel<<<(unsigned)((threads + bs - 1) / bs), bs, 0, s>>>(sh, ia, ja, a, MF, st);
+}
+
+void launch_logdet_reduce(const double* parts, int nparts, double* out, cudaStream_t s) {
+  logdet_reduce_kernel<<<1, 32, 0, s>>>(parts, nparts, out);
+}
+
+void launch_extract_diag(const BtaShape& sh, const double* MS, double* diag, cudaStream_t s) {
+  extract_diag_kernel<<<(unsigned)((sh.n + 255) / 256), 256, 0, s>>>(sh, MS, diag);
+}
+
+void launch_set_identity(double* X, long long ld, int m, int batch, long long stride,
+                         cudaStream_t s) {
+  if (m <= 0 || batch <= 0) return;
+  dim3 grid((m + 31) / 32, (m + 7) / 8, batch);
+  set_identity_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ld, m, stride);
+}
+
+void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,
+                 int batch, long long sX, long long sY, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || batch <= 0) return;
+  dim3 grid((m + 31) / 32, (n + 7) / 8, batch);
+  copy_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ldx, Y, ldy, m, n, sX, sY);
+}
+
+void launch_zero_upper(double* X, long long ld, int m, int batch, long long stride,
+                       cudaStream_t s) {
+  if (m <= 0 || batch <= 0) return;
+  dim3 grid((m + 31) / 32, (m + 7) / 8, batch);
+  zero_upper_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ld, m, stride);
+}
+
+void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
+                     const double* x, const double* b, double* scratch, double* out,
+                     cudaStream_t s) {
+  cudaMemsetAsync(scratch, 0, sizeof(double) * n, s);
+  const long long threads = n * 32;
+  sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, scratch);
+  residual_norm_kernel<<<1, 1024, 0, s>>>(n, b, scratch, out);
+}
+
+void launch_arrow_gemv(const BtaShape& sh, const double* MF, const double* rhs, long long ldr,
+                       int nrhs, double* partial, cudaStream_t s) {
+  if (sh.nd <= 0) return;
+  arrow_gemv_kernel<<<(unsigned)sh.nt, 256, 0, s>>>(sh, MF, rhs, ldr, nrhs, partial);
+}
+
+void launch_arrow_reduce(const BtaShape& sh, const double* partial, int nrhs, double* rhs,
+                         long long ldr, cudaStream_t s) {
+  if (sh.nd <= 0) return;
+  const int p = (int)(sh.nd * nrhs);
+  arrow_reduce_kernel<<<(p + 127) / 128, 128, 0, s>>>(sh, partial, nrhs, rhs, ldr);
+}
+
+}  // namespace rgf

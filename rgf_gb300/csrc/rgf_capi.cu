@@ -1,0 +1,835 @@
+// Host engine and C ABI of librgf_gb300.
+//
+// A handle owns, in device memory: the CSC (uploaded once), the factor in the
+// reference's block-column layout MF, the selected inverse in the same
+// layout, and workspaces.  Each stage (factorize, selected inversion, solve
+// with a given nrhs) is issued once on the handle's stream under CUDA graph
+// capture and replayed afterwards, so the launch sequence costs one graph
+// launch per call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "../../include/rgf.h"
+#include "rgf_internal.h"
+#include "rgf_split.h"
+
+using namespace rgf;
+
+namespace {
+constexpr int NB = 64;  // leaf tile of the FP64 panel Cholesky / triangular solves
+}
+
+struct rgf_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  BtaShape sh{};
+  long long nnz = 0, mf_size = 0;
+  rgf_opts opts{};
+
+  size_t* d_ia = nullptr;
+  size_t* d_ja = nullptr;
+  double* d_a = nullptr;
+  double* d_MF = nullptr;
+  double* d_MS = nullptr;
+  double* d_U = nullptr;     // Linv^T of every diagonal block (ns x ns each), then the corner
+  double* d_T1 = nullptr;    // ns x ns
+  double* d_T2 = nullptr;    // ns x ns
+  double* d_T3 = nullptr;    // nd x ns
+  double* d_logpart = nullptr;
+  int nparts = 0;
+  double* d_scalars = nullptr;  // [0] logdet, [1] ||r||, [2] ||b||
+  double* d_diag = nullptr;
+  DevStatus* d_status = nullptr;
+  double* d_rhs = nullptr;
+  size_t rhs_cap = 0;           // doubles
+  double* d_partial = nullptr;  // arrowhead partial sums, nt * nrhs * nd
+  size_t partial_cap = 0;
+  double* d_res = nullptr;      // residual scratch: x, b, y (3n)
+
+  bool factored = false;
+  bool selinv_done = false;
+  int not_spd_col = -1;
+  size_t device_bytes = 0;
+
+  cudaGraphExec_t g_factor = nullptr, g_selinv = nullptr;
+  long long k_factor = 0, k_selinv = 0;
+  std::map<size_t, std::pair<cudaGraphExec_t, long long>> g_solve;
+  long long kernels_issued = 0;   // kernels of the stage being recorded
+  long long kernels_total = 0;    // kernels launched over the handle's life
+
+  SplitEngine* split = nullptr;
+
+  bool timer_on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_pool;
+  std::vector<double> ev_flops;
+  double timer_ms = 0.0, timer_flops = 0.0;
+  long long timer_launches = 0;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return RGF_OK;
+  if (e == cudaErrorMemoryAllocation) return RGF_ENOMEM;
+  return RGF_ECUDA;
+}
+
+#define RGF_CK(call)                       \
+  do {                                     \
+    cudaError_t e_ = (call);               \
+    if (e_ != cudaSuccess) {               \
+      return cuda_status(e_);              \
+    }                                      \
+  } while (0)
+
+__global__ void status_init_kernel(DevStatus* st) {
+  st->not_spd_col = INT_MAX;
+  st->bad_input = 0;
+  st->timeout = 0;
+}
+
+template <class T>
+int dalloc(rgf_handle* h, T** p, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? RGF_ENOMEM : RGF_ECUDA;
+  }
+  h->device_bytes += count * sizeof(T);
+  return RGF_OK;
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+// ---- launch wrappers (count kernels; optional event timer on bulk GEMMs) ----
+void gemm(rgf_handle* h, const GemmDesc& g, bool bulk) {
+  if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (h->timer_on && bulk) {
+    if (h->ev_pool.empty()) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+    } else {
+      e0 = h->ev_pool.back().first;
+      e1 = h->ev_pool.back().second;
+      h->ev_pool.pop_back();
+    }
+    cudaEventRecord(e0, h->stream);
+  }
+  long long launched = 1;
+  if (h->split && bulk && g.k >= h->split->min_k())
+    launched = h->split->gemm(g, h->stream);
+  else
+    launch_gemm_fp64(g, h->stream);
+  h->kernels_issued += launched;
+  if (e0) {
+    cudaEventRecord(e1, h->stream);
+    h->ev_used.push_back({e0, e1});
+    h->ev_flops.push_back(gemm_flops(g));
+  }
+}
+
+void leaf_potrf(rgf_handle* h, double* T, long long ldt, int nbk, int col0, double* part) {
+  launch_leaf_potrf(T, ldt, nbk, col0, part, h->d_status, h->stream);
+  h->kernels_issued++;
+}
+
+void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
+               const double* L, long long ldl, int nbk, int mode, int batch = 1,
+               long long sX = 0, long long sL = 0) {
+  if (rows <= 0) return;
+  launch_trsm_rows(X, xrs, xcs, rows, L, ldl, nbk, mode, batch, sX, sL, h->stream);
+  h->kernels_issued++;
+}
+
+// ---- panel Cholesky: [D; B; C] (rows x cols, lda) -> [L; B L^-T; C L^-T] ----
+// Right-looking blocked Cholesky of the top cols x cols block with the TRSM
+// of the rows below folded into each column step (RGF.H:254-260, 284-287,
+// 312-317, 335 as one pass).
+void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int col0,
+                 int part0) {
+  int part = part0;
+  for (int k0 = 0; k0 < cols; k0 += NB) {
+    const int nbk = std::min(NB, cols - k0);
+    double* Pkk = P + k0 + (long long)k0 * lda;
+    leaf_potrf(h, Pkk, lda, nbk, col0 + k0, h->d_logpart + part++);
+    const int below = rows - (k0 + nbk);
+    if (below > 0) trsm_rows(h, Pkk + nbk, 1, lda, below, Pkk, lda, nbk, 0);
+    const int rem = cols - (k0 + nbk);
+    if (rem > 0) {
+      GemmDesc g;
+      g.m = below; g.n = rem; g.k = nbk;
+      g.A = Pkk + nbk; g.lda = lda; g.transA = 0;
+      g.B = Pkk + nbk; g.ldb = lda; g.transB = 1;
+      g.C = g.D = P + (k0 + nbk) + (long long)(k0 + nbk) * lda;
+      g.ldc = g.ldd = lda;
+      g.alpha = -1.0; g.beta = 1.0; g.outLower = 1;
+      gemm(h, g, true);
+    }
+  }
+}
+
+// ---- stage 1: factorize (RGF.H:233-340) ----
+void issue_factor(rgf_handle* h) {
+  const BtaShape& sh = h->sh;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
+  cudaStream_t s = h->stream;
+  status_init_kernel<<<1, 1, 0, s>>>(h->d_status);
+  cudaMemsetAsync(h->d_MF, 0, sizeof(double) * h->mf_size, s);
+  launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, s);
+  h->kernels_issued += 2;
+  double* corner = h->d_MF + mf_col_offset(sh, nt);
+  const int tiles = (int)((ns + NB - 1) / NB);
+  for (long long i = 0; i < nt; ++i) {
+    double* P = h->d_MF + mf_col_offset(sh, i);
+    const long long lda = mf_lda(sh, i);
+    if (i > 0) {
+      const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
+      const long long ldm = mf_lda(sh, i - 1);
+      GemmDesc g;  // D_i -= L_{i,i-1} L_{i,i-1}^T   (RGF.H:276, 304)
+      g.m = g.n = g.k = (int)ns;
+      g.A = Pm + ns; g.lda = ldm; g.B = Pm + ns; g.ldb = ldm; g.transB = 1;
+      g.C = g.D = P; g.ldc = g.ldd = lda;
+      g.alpha = -1.0; g.beta = 1.0; g.outLower = 1;
+      gemm(h, g, true);
+      if (nd > 0) {
+        const double* Cm = Pm + mf_dense_row(sh, i - 1);
+        GemmDesc a;  // C_i -= C_{i-1} L_{i,i-1}^T  (RGF.H:279, 307)
+        a.m = (int)nd; a.n = (int)ns; a.k = (int)ns;
+        a.A = Cm; a.lda = ldm; a.B = Pm + ns; a.ldb = ldm; a.transB = 1;
+        a.C = a.D = P + mf_dense_row(sh, i); a.ldc = a.ldd = lda;
+        a.alpha = -1.0; a.beta = 1.0;
+        gemm(h, a, true);
+        GemmDesc c;  // corner -= C_{i-1} C_{i-1}^T  (RGF.H:280, 308)
+        c.m = c.n = (int)nd; c.k = (int)ns;
+        c.A = Cm; c.lda = ldm; c.B = Cm; c.ldb = ldm; c.transB = 1;
+        c.C = c.D = corner; c.ldc = c.ldd = nd;
+        c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
+        gemm(h, c, false);
+      }
+    }
+    panel_potrf(h, P, lda, (int)lda, (int)ns, (int)(i * ns), (int)(i * tiles));
+  }
+  if (nd > 0) {
+    const double* Pl = h->d_MF + mf_col_offset(sh, nt - 1);
+    const double* Cl = Pl + mf_dense_row(sh, nt - 1);
+    GemmDesc c;  // corner -= C_{nt-1} C_{nt-1}^T  (RGF.H:332)
+    c.m = c.n = (int)nd; c.k = (int)ns;
+    c.A = Cl; c.lda = mf_lda(sh, nt - 1); c.B = Cl; c.ldb = mf_lda(sh, nt - 1); c.transB = 1;
+    c.C = c.D = corner; c.ldc = c.ldd = nd;
+    c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
+    gemm(h, c, false);
+    panel_potrf(h, corner, nd, (int)nd, (int)nd, (int)(nt * ns), (int)(nt * tiles));  // RGF.H:335
+  }
+  launch_logdet_reduce(h->d_logpart, h->nparts, h->d_scalars, s);
+  h->kernels_issued++;
+}
+
+// For every diagonal block at once: U_i = L_ii^{-T} (upper triangular).
+// Right-looking RLTN solve U L^T = I by 64-column blocks; only rows above the
+// current block are non-zero, so the work is ns^3/3 per block.  The
+// nt-1 blocks of leading dimension 2ns+nd run as one batch, the last block
+// (leading dimension ns+nd) and the corner separately.
+void issue_trtri(rgf_handle* h, double* U, long long ldu, long long m, const double* L,
+                 long long ldl, int batch, long long sU, long long sL) {
+  if (batch <= 0 || m <= 0) return;
+  launch_set_identity(U, ldu, (int)m, batch, sU, h->stream);
+  h->kernels_issued++;
+  for (long long k0 = 0; k0 < m; k0 += NB) {
+    const int nbk = (int)std::min<long long>(NB, m - k0);
+    trsm_rows(h, U + k0 * ldu, 1, ldu, (int)(k0 + nbk), L + k0 + k0 * ldl, ldl, nbk, 0, batch,
+              sU, sL);
+    const long long rem = m - k0 - nbk;
+    if (rem > 0) {
+      GemmDesc g;
+      g.m = (int)(k0 + nbk); g.n = (int)rem; g.k = nbk;
+      g.A = U + k0 * ldu; g.lda = ldu;
+      g.B = L + (k0 + nbk) + k0 * ldl; g.ldb = ldl; g.transB = 1;
+      g.C = g.D = U + (k0 + nbk) * ldu; g.ldc = g.ldd = ldu;
+      g.alpha = -1.0; g.beta = 1.0;
+      g.batch = batch; g.sA = sU; g.sB = sL; g.sC = g.sD = sU;
+      gemm(h, g, true);
+    }
+  }
+}
+
+GemmDesc mk(int m, int n, int k, const double* A, long long lda, int tA, const double* B,
+            long long ldb, int tB, const double* C, long long ldc, double* D, long long ldd,
+            double alpha, double beta) {
+  GemmDesc g;
+  g.m = m; g.n = n; g.k = k;
+  g.A = A; g.lda = lda; g.transA = tA;
+  g.B = B; g.ldb = ldb; g.transB = tB;
+  g.C = C; g.ldc = ldc; g.D = D; g.ldd = ldd;
+  g.alpha = alpha; g.beta = beta;
+  return g;
+}
+
+// ---- stage 3: selected inversion ----
+void issue_selinv(rgf_handle* h) {
+  const BtaShape& sh = h->sh;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
+  const int ins = (int)ns, ind = (int)nd;
+  cudaStream_t s = h->stream;
+  const long long ss = ns * ns;
+  double* Ud = h->d_U + nt * ss;
+  double* Sdd = h->d_MS + mf_col_offset(sh, nt);
+  // batched inverses of all diagonal blocks
+  if (nt > 1)
+    issue_trtri(h, h->d_U, ns, ns, h->d_MF, 2 * ns + nd, (int)(nt - 1), ss, ns * (2 * ns + nd));
+  issue_trtri(h, h->d_U + (nt - 1) * ss, ns, ns, h->d_MF + mf_col_offset(sh, nt - 1), ns + nd, 1,
+              0, 0);
+  if (nd > 0) {
+    issue_trtri(h, Ud, nd, nd, h->d_MF + mf_col_offset(sh, nt), nd, 1, 0, 0);
+    // Sigma_dd = L_dd^{-T} L_dd^{-1} = U_d U_d^T   (RGF.H:439-442)
+    gemm(h, mk(ind, ind, ind, Ud, nd, 0, Ud, nd, 1, nullptr, 0, Sdd, nd, 1.0, 0.0), false);
+  }
+  const bool compat = h->opts.selinv_mode == RGF_SELINV_COMPAT;
+  for (long long i = nt - 1; i >= 0; --i) {
+    const double* P = h->d_MF + mf_col_offset(sh, i);
+    double* Q = h->d_MS + mf_col_offset(sh, i);
+    const long long lda = mf_lda(sh, i);
+    const double* Ui = h->d_U + i * ss;
+    const double* Bi = P + ns;                      // L_{i+1,i}
+    const double* Ci = P + mf_dense_row(sh, i);     // C_i
+    const bool has_next = i < nt - 1;
+    const double* Sn = has_next ? h->d_MS + mf_col_offset(sh, i + 1) : nullptr;  // Sigma_{i+1,i+1}
+    const long long ldn = has_next ? mf_lda(sh, i + 1) : 0;
+    const double* Sdn = has_next ? Sn + mf_dense_row(sh, i + 1) : nullptr;       // Sigma_{d,i+1}
+    if (!compat) {
+      if (has_next) {
+        // X = Sigma_{i+1,i+1} L_{i+1,i} + Sigma_{d,i+1}^T C_i
+        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), true);
+        if (nd > 0)
+          gemm(h, mk(ins, ins, ind, Sdn, ldn, 1, Ci, lda, 0, h->d_T1, ns, h->d_T1, ns, 1.0, 1.0),
+               false);
+        // Sigma_{i+1,i} = -X L_ii^{-1} = -X U_i^T
+        GemmDesc g = mk(ins, ins, ins, h->d_T1, ns, 0, Ui, ns, 1, nullptr, 0, Q + ns, lda, -1.0, 0.0);
+        g.triB = TRI_LOWER;
+        gemm(h, g, true);
+      }
+      if (nd > 0) {
+        // Y = Sigma_dd C_i + Sigma_{d,i+1} L_{i+1,i};  Sigma_{d,i} = -Y U_i^T
+        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), false);
+        if (has_next)
+          gemm(h, mk(ind, ins, ins, Sdn, ldn, 0, Bi, lda, 0, h->d_T3, nd, h->d_T3, nd, 1.0, 1.0),
+               true);
+        GemmDesc g = mk(ind, ins, ins, h->d_T3, nd, 0, Ui, ns, 1, nullptr, 0,
+                        Q + mf_dense_row(sh, i), lda, -1.0, 0.0);
+        g.triB = TRI_LOWER;
+        gemm(h, g, true);
+      }
+      // W^T = U_i - Sigma_{i+1,i}^T L_{i+1,i} - Sigma_{d,i}^T C_i
+      if (has_next) {
+        gemm(h, mk(ins, ins, ins, Q + ns, lda, 1, Bi, lda, 0, Ui, ns, h->d_T2, ns, -1.0, 1.0), true);
+      } else {
+        launch_copy(Ui, ns, h->d_T2, ns, ins, ins, 1, 0, 0, s);
+        h->kernels_issued++;
+      }
+      if (nd > 0)
+        gemm(h, mk(ins, ins, ind, Q + mf_dense_row(sh, i), lda, 1, Ci, lda, 0, h->d_T2, ns,
+                   h->d_T2, ns, -1.0, 1.0), false);
+      // Sigma_ii = L_ii^{-T} W = U_i (W^T)^T
+      GemmDesc g = mk(ins, ins, ins, Ui, ns, 0, h->d_T2, ns, 1, nullptr, 0, Q, lda, 1.0, 0.0);
+      g.triA = TRI_UPPER;
+      gemm(h, g, true);
+    } else {
+      // the reference's recursion (RGF.H:444-502):
+      // Sigma_ii = L^{-T} (I + B^T Sigma_{i+1,i+1} B + C^T Sigma_dd C) L^{-1}
+      launch_set_identity(h->d_T2, ns, ins, 1, 0, s);
+      h->kernels_issued++;
+      if (has_next) {
+        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), true);
+        gemm(h, mk(ins, ins, ins, Bi, lda, 1, h->d_T1, ns, 0, h->d_T2, ns, h->d_T2, ns, 1.0, 1.0),
+             true);
+      }
+      if (nd > 0) {
+        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), false);
+        gemm(h, mk(ins, ins, ind, Ci, lda, 1, h->d_T3, nd, 0, h->d_T2, ns, h->d_T2, ns, 1.0, 1.0),
+             false);
+      }
+      GemmDesc g1 = mk(ins, ins, ins, h->d_T2, ns, 0, Ui, ns, 1, nullptr, 0, h->d_T1, ns, 1.0, 0.0);
+      g1.triB = TRI_LOWER;
+      gemm(h, g1, true);
+      GemmDesc g2 = mk(ins, ins, ins, Ui, ns, 0, h->d_T1, ns, 0, nullptr, 0, Q, lda, 1.0, 0.0);
+      g2.triA = TRI_UPPER;
+      gemm(h, g2, true);
+    }
+  }
+  launch_extract_diag(sh, h->d_MS, h->d_diag, s);
+  h->kernels_issued++;
+}
+
+// L X = R (left, lower, no transpose) for the ns x nrhs block R (ld ldr).
+void trsv_lower(rgf_handle* h, const double* L, long long ldl, int m, double* R, long long ldr,
+                int nrhs) {
+  for (int k0 = 0; k0 < m; k0 += NB) {
+    const int nbk = std::min(NB, m - k0);
+    const double* Lkk = L + k0 + (long long)k0 * ldl;
+    trsm_rows(h, R + k0, ldr, 1, nrhs, Lkk, ldl, nbk, 0);
+    const int rem = m - k0 - nbk;
+    if (rem > 0)
+      gemm(h, mk(rem, nrhs, nbk, Lkk + nbk, ldl, 0, R + k0, ldr, 0, R + k0 + nbk, ldr,
+                 R + k0 + nbk, ldr, -1.0, 1.0), false);
+  }
+}
+
+// L^T X = R (left, lower, transposed).
+void trsv_lower_t(rgf_handle* h, const double* L, long long ldl, int m, double* R, long long ldr,
+                  int nrhs) {
+  const int nblk = (m + NB - 1) / NB;
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int k0 = b * NB;
+    const int nbk = std::min(NB, m - k0);
+    const double* Lkk = L + k0 + (long long)k0 * ldl;
+    trsm_rows(h, R + k0, ldr, 1, nrhs, Lkk, ldl, nbk, 1);
+    if (k0 > 0)
+      gemm(h, mk(k0, nrhs, nbk, L + k0, ldl, 1, R + k0, ldr, 0, R, ldr, R, ldr, -1.0, 1.0), false);
+  }
+}
+
+// ---- stage 2: solve (RGF.H:344-418) on the device buffer d_rhs ----
+void issue_solve(rgf_handle* h, int nrhs) {
+  const BtaShape& sh = h->sh;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd, n = sh.n;
+  const int ins = (int)ns, ind = (int)nd;
+  double* R = h->d_rhs;
+  const double* corner = h->d_MF + mf_col_offset(sh, nt);
+  for (long long i = 0; i < nt; ++i) {
+    const double* P = h->d_MF + mf_col_offset(sh, i);
+    const long long lda = mf_lda(sh, i);
+    if (i > 0) {
+      const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
+      gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 0, R + (i - 1) * ns, n, 0,
+                 R + i * ns, n, R + i * ns, n, -1.0, 1.0), false);       // RGF.H:365
+    }
+    trsv_lower(h, P, lda, ins, R + i * ns, n, nrhs);                      // RGF.H:356,367
+  }
+  if (nd > 0) {
+    launch_arrow_gemv(sh, h->d_MF, R, n, nrhs, h->d_partial, h->stream);  // RGF.H:377-380
+    launch_arrow_reduce(sh, h->d_partial, nrhs, R, n, h->stream);
+    h->kernels_issued += 2;
+    trsv_lower(h, corner, nd, ind, R + nt * ns, n, nrhs);                 // RGF.H:382
+    trsv_lower_t(h, corner, nd, ind, R + nt * ns, n, nrhs);               // RGF.H:393
+    // rhs_i -= C_i^T rhs_d for every block column (RGF.H:396-399)
+    if (nt > 1) {
+      GemmDesc g = mk(ins, nrhs, ind, h->d_MF + 2 * ns, 2 * ns + nd, 1, R + nt * ns, n, 0, R, n, R,
+                      n, -1.0, 1.0);
+      g.batch = (int)(nt - 1); g.sA = ns * (2 * ns + nd); g.sB = 0; g.sC = g.sD = ns;
+      gemm(h, g, false);
+    }
+    const double* Pl = h->d_MF + mf_col_offset(sh, nt - 1);
+    gemm(h, mk(ins, nrhs, ind, Pl + ns, ns + nd, 1, R + nt * ns, n, 0, R + (nt - 1) * ns, n,
+               R + (nt - 1) * ns, n, -1.0, 1.0), false);
+  }
+  for (long long i = nt - 1; i >= 0; --i) {
+    const double* P = h->d_MF + mf_col_offset(sh, i);
+    trsv_lower_t(h, P, mf_lda(sh, i), ins, R + i * ns, n, nrhs);          // RGF.H:408,417
+    if (i > 0) {
+      const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
+      gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 1, R + i * ns, n, 0,
+                 R + (i - 1) * ns, n, R + (i - 1) * ns, n, -1.0, 1.0), false);  // RGF.H:410
+    }
+  }
+}
+
+// ---- graph capture / replay ----
+template <class F>
+int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, F issue) {
+  if (h->timer_on || !h->opts.use_graphs) {
+    h->kernels_issued = 0;
+    issue();
+    h->kernels_total += h->kernels_issued;
+    RGF_CK(cudaGetLastError());
+    return RGF_OK;
+  }
+  if (!*exec) {
+    cudaGraph_t graph = nullptr;
+    h->kernels_issued = 0;
+    RGF_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    issue();
+    cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (e != cudaSuccess) return cuda_status(e);
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      *exec = nullptr;
+      return cuda_status(e);
+    }
+    *nk = h->kernels_issued;
+  }
+  RGF_CK(cudaGraphLaunch(*exec, h->stream));
+  h->kernels_total += *nk;
+  return RGF_OK;
+}
+
+int collect_timer(rgf_handle* h) {
+  for (size_t i = 0; i < h->ev_used.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev_used[i].first, h->ev_used[i].second);
+    h->timer_ms += ms;
+    h->timer_flops += h->ev_flops[i];
+    h->timer_launches++;
+    h->ev_pool.push_back(h->ev_used[i]);
+  }
+  h->ev_used.clear();
+  h->ev_flops.clear();
+  return RGF_OK;
+}
+
+int sync_and_check(rgf_handle* h) {
+  RGF_CK(cudaStreamSynchronize(h->stream));
+  RGF_CK(cudaGetLastError());
+  if (h->timer_on) collect_timer(h);
+  DevStatus st;
+  RGF_CK(cudaMemcpy(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st.timeout) return RGF_ETIMEOUT;
+  if (st.bad_input) return RGF_EINVAL;
+  if (st.not_spd_col != INT_MAX) {
+    h->not_spd_col = st.not_spd_col;
+    return RGF_ENOTSPD;
+  }
+  h->not_spd_col = -1;
+  return RGF_OK;
+}
+
+int ensure_factored(rgf_handle* h) {
+  if (h->factored) return RGF_OK;
+  int st = run_stage(h, &h->g_factor, &h->k_factor, [&] { issue_factor(h); });
+  if (st) return st;
+  st = sync_and_check(h);
+  if (st) return st;
+  h->factored = true;
+  h->selinv_done = false;
+  return RGF_OK;
+}
+
+int ensure_selinv(rgf_handle* h) {
+  int st = ensure_factored(h);
+  if (st) return st;
+  if (h->selinv_done) return RGF_OK;
+  if (!h->d_MS) {
+    const long long ns = h->sh.ns, nt = h->sh.nt, nd = h->sh.nd;
+    if ((st = dalloc(h, &h->d_MS, h->mf_size))) return st;
+    if ((st = dalloc(h, &h->d_U, nt * ns * ns + nd * nd))) return st;
+    if ((st = dalloc(h, &h->d_T1, ns * ns))) return st;
+    if ((st = dalloc(h, &h->d_T2, ns * ns))) return st;
+    if ((st = dalloc(h, &h->d_T3, std::max<long long>(1, nd * ns)))) return st;
+    RGF_CK(cudaMemsetAsync(h->d_MS, 0, sizeof(double) * h->mf_size, h->stream));
+  }
+  st = run_stage(h, &h->g_selinv, &h->k_selinv, [&] { issue_selinv(h); });
+  if (st) return st;
+  st = sync_and_check(h);
+  if (st) return st;
+  h->selinv_done = true;
+  return RGF_OK;
+}
+
+int validate_host_csc(const size_t* ia, long long n) {
+  if (ia[0] != 0) return RGF_EINVAL;
+  for (long long c = 0; c < n; ++c)
+    if (ia[c + 1] < ia[c]) return RGF_EINVAL;
+  return RGF_OK;
+}
+
+void release(rgf_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->g_factor) cudaGraphExecDestroy(h->g_factor);
+  if (h->g_selinv) cudaGraphExecDestroy(h->g_selinv);
+  for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
+  for (auto& e : h->ev_used) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& e : h->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  delete h->split;
+  void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
+                  h->d_logpart, h->d_scalars, h->d_diag, h->d_status, h->d_rhs, h->d_partial,
+                  h->d_res};
+  for (void* p : bufs) dfree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char* rgf_status_string(int status) {
+  switch (status) {
+    case RGF_OK: return "RGF_OK";
+    case RGF_EINVAL: return "RGF_EINVAL: invalid argument or CSC outside the block pattern";
+    case RGF_ENOMEM: return "RGF_ENOMEM: device allocation failed";
+    case RGF_ENOTSPD: return "RGF_ENOTSPD: matrix is not positive definite";
+    case RGF_ECUDA: return "RGF_ECUDA: CUDA error or no usable device";
+    case RGF_ETIMEOUT: return "RGF_ETIMEOUT: a bounded device wait gave up";
+    case RGF_ENOTSUP: return "RGF_ENOTSUP: option not supported";
+    default: return "unknown rgf status";
+  }
+}
+
+int rgf_default_opts(rgf_opts* o) {
+  if (!o) return RGF_EINVAL;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = RGF_PREC_FP64;
+  o->slices = 0;
+  o->selinv_mode = RGF_SELINV_EXACT;
+  o->device = -1;
+  o->use_graphs = 1;
+  return RGF_OK;
+}
+
+int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, size_t nt,
+               size_t nd, const rgf_opts* opts, rgf_handle** out) {
+  if (!out) return RGF_EINVAL;
+  *out = nullptr;
+  if (!ia || !ja || !a || ns < 1 || nt < 1) return RGF_EINVAL;
+  if (ns > (1u << 20) || nd > (1u << 20) || nt > (1u << 24)) return RGF_EINVAL;
+  const long long n = (long long)(ns * nt + nd);
+  if (n >= INT_MAX) return RGF_EINVAL;
+  if (validate_host_csc(ia, n)) return RGF_EINVAL;
+  rgf_opts o;
+  rgf_default_opts(&o);
+  if (opts) o = *opts;
+  if (o.precision != RGF_PREC_FP64 && o.precision != RGF_PREC_SPLIT) return RGF_EINVAL;
+  if (o.selinv_mode != RGF_SELINV_EXACT && o.selinv_mode != RGF_SELINV_COMPAT) return RGF_EINVAL;
+  if (o.slices < 0 || o.slices > 16) return RGF_EINVAL;
+
+  int dev = o.device;
+  if (dev < 0) {
+    if (cudaGetDevice(&dev) != cudaSuccess) return RGF_ECUDA;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || dev >= ndev) {
+    cudaGetLastError();
+    return RGF_ECUDA;
+  }
+  if (cudaSetDevice(dev) != cudaSuccess) return RGF_ECUDA;
+
+  rgf_handle* h = new (std::nothrow) rgf_handle();
+  if (!h) return RGF_ENOMEM;
+  h->device = dev;
+  h->opts = o;
+  h->sh = {(long long)ns, (long long)nt, (long long)nd, n};
+  h->nnz = (long long)ia[n];
+  h->mf_size = 2 * (long long)(nt - 1) * ns * ns + (long long)ns * ns + n * (long long)nd;
+  int st = RGF_OK;
+  do {
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      st = RGF_ECUDA;
+      break;
+    }
+    if ((st = dalloc(h, &h->d_ia, n + 1))) break;
+    if ((st = dalloc(h, &h->d_ja, h->nnz))) break;
+    if ((st = dalloc(h, &h->d_a, h->nnz))) break;
+    if ((st = dalloc(h, &h->d_MF, h->mf_size))) break;
+    const int tiles = (int)((ns + NB - 1) / NB), dtiles = (int)((nd + NB - 1) / NB);
+    h->nparts = (int)(nt * tiles + dtiles);
+    if ((st = dalloc(h, &h->d_logpart, h->nparts))) break;
+    if ((st = dalloc(h, &h->d_scalars, 8))) break;
+    if ((st = dalloc(h, &h->d_diag, n))) break;
+    if ((st = dalloc(h, &h->d_status, 1))) break;
+    if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice, h->stream) ||
+        cudaMemcpyAsync(h->d_ja, ja, sizeof(size_t) * h->nnz, cudaMemcpyHostToDevice, h->stream) ||
+        cudaMemcpyAsync(h->d_a, a, sizeof(double) * h->nnz, cudaMemcpyHostToDevice, h->stream)) {
+      st = RGF_ECUDA;
+      break;
+    }
+    if (o.precision == RGF_PREC_SPLIT) {
+      h->split = SplitEngine::create(o.slices, &st);
+      if (st) break;
+    }
+    // validate the pattern once on the device
+    status_init_kernel<<<1, 1, 0, h->stream>>>(h->d_status);
+    cudaMemsetAsync(h->d_MF, 0, sizeof(double) * h->mf_size, h->stream);
+    launch_ingest(h->sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, h->stream);
+    st = sync_and_check(h);
+  } while (0);
+  if (st) {
+    release(h);
+    return st;
+  }
+  *out = h;
+  return RGF_OK;
+}
+
+int rgf_destroy(rgf_handle* h) {
+  if (!h) return RGF_EINVAL;
+  release(h);
+  return RGF_OK;
+}
+
+int rgf_factorize(rgf_handle* h) {
+  if (!h) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  h->factored = false;
+  h->selinv_done = false;
+  return ensure_factored(h);
+}
+
+int rgf_logdet(rgf_handle* h, double* logdet) {
+  if (!h || !logdet) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  int st = ensure_factored(h);
+  if (st) return st;
+  RGF_CK(cudaMemcpy(logdet, h->d_scalars, sizeof(double), cudaMemcpyDeviceToHost));
+  return RGF_OK;
+}
+
+int rgf_diag(rgf_handle* h, double* diag) {
+  if (!h || !diag) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  int st = ensure_selinv(h);
+  if (st) return st;
+  RGF_CK(cudaMemcpy(diag, h->d_diag, sizeof(double) * h->sh.n, cudaMemcpyDeviceToHost));
+  return RGF_OK;
+}
+
+int rgf_diag_device(rgf_handle* h, const double** d_diag) {
+  if (!h || !d_diag) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  int st = ensure_selinv(h);
+  if (st) return st;
+  *d_diag = h->d_diag;
+  return RGF_OK;
+}
+
+int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
+  if (!h || !x || !b) return RGF_EINVAL;
+  if (nrhs == 0) return RGF_OK;
+  if (nrhs > 4096) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  int st = ensure_factored(h);
+  if (st) return st;
+  const long long n = h->sh.n;
+  const size_t need = (size_t)n * nrhs;
+  if (need > h->rhs_cap) {
+    for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
+    h->g_solve.clear();
+    dfree(h->d_rhs);
+    h->device_bytes -= h->rhs_cap * sizeof(double);
+    h->rhs_cap = 0;
+    if ((st = dalloc(h, &h->d_rhs, need))) return st;
+    h->rhs_cap = need;
+  }
+  const size_t pneed = (size_t)h->sh.nt * nrhs * std::max<long long>(1, h->sh.nd);
+  if (pneed > h->partial_cap) {
+    for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
+    h->g_solve.clear();
+    dfree(h->d_partial);
+    h->device_bytes -= h->partial_cap * sizeof(double);
+    h->partial_cap = 0;
+    if ((st = dalloc(h, &h->d_partial, pneed))) return st;
+    h->partial_cap = pneed;
+  }
+  RGF_CK(cudaMemcpyAsync(h->d_rhs, b, sizeof(double) * need, cudaMemcpyHostToDevice, h->stream));
+  auto it = h->g_solve.find(nrhs);
+  cudaGraphExec_t exec = it == h->g_solve.end() ? nullptr : it->second.first;
+  long long nk = it == h->g_solve.end() ? 0 : it->second.second;
+  st = run_stage(h, &exec, &nk, [&] { issue_solve(h, (int)nrhs); });
+  if (st) return st;
+  if (exec) h->g_solve[nrhs] = {exec, nk};
+  RGF_CK(cudaMemcpyAsync(x, h->d_rhs, sizeof(double) * need, cudaMemcpyDeviceToHost, h->stream));
+  return sync_and_check(h);
+}
+
+int rgf_residual_norm(rgf_handle* h, const double* x, const double* b, double* norm) {
+  if (!h || !x || !b || !norm) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  const long long n = h->sh.n;
+  int st;
+  if (!h->d_res && (st = dalloc(h, &h->d_res, 3 * n))) return st;
+  RGF_CK(cudaMemcpyAsync(h->d_res, x, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  RGF_CK(cudaMemcpyAsync(h->d_res + n, b, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  launch_residual(n, h->d_ia, h->d_ja, h->d_a, h->d_res, h->d_res + n, h->d_res + 2 * n,
+                  h->d_scalars + 1, h->stream);
+  double out[2];
+  RGF_CK(cudaMemcpyAsync(out, h->d_scalars + 1, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
+  RGF_CK(cudaStreamSynchronize(h->stream));
+  RGF_CK(cudaGetLastError());
+  *norm = out[0];
+  return RGF_OK;
+}
+
+int rgf_residual_norm_normalized(rgf_handle* h, const double* x, const double* b, double* norm) {
+  if (!h || !x || !b || !norm) return RGF_EINVAL;
+  double r;
+  int st = rgf_residual_norm(h, x, b, &r);
+  if (st) return st;
+  double out[2];
+  RGF_CK(cudaMemcpy(out, h->d_scalars + 1, sizeof(out), cudaMemcpyDeviceToHost));
+  *norm = out[0] / out[1];
+  return RGF_OK;
+}
+
+int rgf_export_factor(rgf_handle* h, double* mf) {
+  if (!h || !mf) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  int st = ensure_factored(h);
+  if (st) return st;
+  RGF_CK(cudaMemcpy(mf, h->d_MF, sizeof(double) * h->mf_size, cudaMemcpyDeviceToHost));
+  return RGF_OK;
+}
+
+int rgf_export_selinv(rgf_handle* h, double* ms) {
+  if (!h || !ms) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  int st = ensure_selinv(h);
+  if (st) return st;
+  RGF_CK(cudaMemcpy(ms, h->d_MS, sizeof(double) * h->mf_size, cudaMemcpyDeviceToHost));
+  return RGF_OK;
+}
+
+int rgf_get_info(rgf_handle* h, rgf_info_t* info) {
+  if (!h || !info) return RGF_EINVAL;
+  std::memset(info, 0, sizeof(*info));
+  info->n = (size_t)h->sh.n;
+  info->nnz = (size_t)h->nnz;
+  info->mf_size = (size_t)h->mf_size;
+  info->device_bytes = h->device_bytes;
+  info->not_spd_column = h->not_spd_col;
+  info->kernels_launched = h->kernels_total;
+  return RGF_OK;
+}
+
+int rgf_get_stream(rgf_handle* h, void** stream) {
+  if (!h || !stream) return RGF_EINVAL;
+  *stream = (void*)h->stream;
+  return RGF_OK;
+}
+
+int rgf_kernel_timer_enable(rgf_handle* h, int enable) {
+  if (!h) return RGF_EINVAL;
+  h->timer_on = enable != 0;
+  return RGF_OK;
+}
+
+int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launches,
+                          double* flops) {
+  if (!h) return RGF_EINVAL;
+  if (ms) *ms = h->timer_ms;
+  if (launches) *launches = h->timer_launches;
+  if (flops) *flops = h->timer_flops;
+  if (reset) {
+    h->timer_ms = 0.0;
+    h->timer_flops = 0.0;
+    h->timer_launches = 0;
+  }
+  return RGF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// Internal interfaces shared by the CUDA translation units of librgf_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace rgf {
+
+// Lives in device memory, one per handle.  Kernels record failures here
+// instead of trapping; the host reads it after each stage.
+struct DevStatus {
+  int not_spd_col;   // smallest global column with a non-positive pivot (INT32_MAX: none)
+  int bad_input;     // ingest saw an entry outside the block pattern
+  int timeout;       // a bounded device-side wait gave up
+  int pad;
+};
+
+enum Tri { TRI_NONE = 0, TRI_LOWER = 1, TRI_UPPER = 2 };
+
+// D = alpha * op(A) * op(B) + beta * C, column-major, op(A) m x k, op(B) k x n.
+// triA/triB declare a triangular operand (of op(X)); its other triangle is
+// treated as zero whatever memory holds.  outLower writes only r >= c.
+// batch > 1 runs independent problems offset by sA/sB/sC/sD elements.
+struct GemmDesc {
+  int m = 0, n = 0, k = 0;
+  const double* A = nullptr; long long lda = 0; int transA = 0;
+  const double* B = nullptr; long long ldb = 0; int transB = 0;
+  const double* C = nullptr; long long ldc = 0;
+  double* D = nullptr; long long ldd = 0;
+  double alpha = 1.0, beta = 0.0;
+  int triA = TRI_NONE, triB = TRI_NONE, outLower = 0;
+  int batch = 1;
+  long long sA = 0, sB = 0, sC = 0, sD = 0;
+};
+
+// Algorithmic flops of one GemmDesc (triangular operands and lower-only
+// outputs counted at their LAPACK sizes).
+double gemm_flops(const GemmDesc& g);
+
+// ---- FP64 kernels (k_fp64.cu) ---------------------------------------------
+void launch_gemm_fp64(const GemmDesc& g, cudaStream_t s);
+
+// Cholesky of the nbk x nbk (nbk <= 64) lower tile at T (column-major, ldt),
+// in place.  Writes sum(log diag) of the tile to *logpart and records the
+// first non-positive pivot (global column col0 + j) in st.
+void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, double* logpart,
+                       DevStatus* st, cudaStream_t s);
+
+// Row-parallel triangular solve with an nbk x nbk (nbk <= 64) lower tile L:
+//   mode 0: X := X * L^{-T}   (forward,  "R L T N")
+//   mode 1: X := X * L^{-1}   (backward, "R L N N")
+// X has `rows` independent rows; element (r, j) at X[r*xrs + j*xcs].
+// batch > 1: problem b uses X + b*sX, L + b*sL.
+void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,
+                      long long ldl, int nbk, int mode, int batch, long long sX, long long sL,
+                      cudaStream_t s);
+
+// ---- small kernels (k_misc.cu) ------------------------------------------------
+struct BtaShape {
+  long long ns, nt, nd, n;
+};
+long long mf_col_offset(const BtaShape& sh, long long i);
+long long mf_lda(const BtaShape& sh, long long i);
+long long mf_dense_row(const BtaShape& sh, long long i);
+
+// Scatter the device CSC into the (pre-zeroed) MF layout; one warp per column.
+void launch_ingest(const BtaShape& sh, const size_t* ia, const size_t* ja, const double* a,
+                   double* MF, DevStatus* st, cudaStream_t s);
+// Sum of nparts partial log sums, times 2, in a fixed order -> *out.
+void launch_logdet_reduce(const double* parts, int nparts, double* out, cudaStream_t s);
+// diag[k] = MS[diag position of k] for all k < n.
+void launch_extract_diag(const BtaShape& sh, const double* MS, double* diag, cudaStream_t s);
+// batch of identity matrices (m x m, ld) at X + b*stride
+void launch_set_identity(double* X, long long ld, int m, int batch, long long stride,
+                         cudaStream_t s);
+// Y (m x n, ldy) = X (m x n, ldx); batched
+void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,
+                 int batch, long long sX, long long sY, cudaStream_t s);
+// zero the strict upper triangle of an m x m block; batched
+void launch_zero_upper(double* X, long long ld, int m, int batch, long long stride,
+                       cudaStream_t s);
+// r = b - A x (symmetric, from the lower CSC) for the first column; then
+// out[0] = ||r||_2, out[1] = ||b||_2.  scratch: n doubles.
+void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
+                     const double* x, const double* b, double* scratch, double* out,
+                     cudaStream_t s);
+// out[q*ldo + dd] = sum_i sum_j C_i(dd, j) * R_i(j, q) over block columns,
+// computed as per-block partials then an ordered sum: the arrowhead part of
+// the forward solve.  y_d -= that.
+void launch_arrow_gemv(const BtaShape& sh, const double* MF, const double* rhs, long long ldr,
+                       int nrhs, double* partial, cudaStream_t s);
+void launch_arrow_reduce(const BtaShape& sh, const double* partial, int nrhs, double* rhs,
+                         long long ldr, cudaStream_t s);
+
+}  // namespace rgf
