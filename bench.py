@@ -1,0 +1,324 @@
+"""Benchmark: factorize + logDet + RGFdiag of one block-tridiagonal-arrowhead
+matrix on GB300, FP64-equivalent TFLOP/s (algorithmic LAPACK flop count).
+
+Workload (default): ns=2000, nt=100, nd=6 (n = 200006), seeded synthetic SPD
+matrix (diagonal blocks A A^T/ns + (ns+2) I, sub-diagonal N(0, 0.1/ns),
+arrowhead N(0, 0.1), corner R R^T/nd + (nt+2) I), stored as the lower CSC
+the reference's RGF constructor takes.  One step = factorize (ingest of the
+device-resident CSC into the block layout, Cholesky recursion, log-sum) +
+logDet + RGFdiag (selected inversion, diag left on the device).
+
+Arms:
+  --impl rgf (default)  this library through its C ABI; prints one JSON line
+                        with value (inputs resident in HBM), e2e (host CSC ->
+                        device, diag back to host, through rgf_create/...),
+                        roofline of the dominant kernel, cpu_baseline, clocks.
+  --impl reference      the CPU restatement of the reference recursion on the
+                        host cores (numpy/scipy OpenBLAS, all threads), on a
+                        bounded sample of the same workload.
+Under torchrun with N > 1 every rank runs an independent replica (the
+recursion does not shard); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "ns2000_nt100_nd6": dict(ns=2000, nt=100, nd=6, seed=3, spde=None),
+    "ns1000_nt50_nd4": dict(ns=1000, nt=50, nd=4, seed=2, spde=(40, 25)),
+    "ns3_nt3_nd2": dict(ns=3, nt=3, nd=2, seed=1, spde=None),
+}
+METRIC = "FP64-equiv TFLOP/s for factorize+logDet+RGFdiag"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax.append(float(p[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(w):
+    from rgf_gb300 import gen
+    t = time.time()
+    ia, ja, a = gen.generate_bta(w["ns"], w["nt"], w["nd"], w["seed"], spde_grid=w["spde"])
+    log(f"[bench] generated n={len(ia) - 1} nnz={len(ja)} in {time.time() - t:.1f}s")
+    return ia, ja, a
+
+
+def cpu_port_sample(w, target_s: float = 12.0):
+    """Time the oracle's block recursion (numpy/scipy, all host threads) on a
+    prefix of the workload's block columns sized for ~target_s seconds.
+    Returns (tflops, cores, sample description, seconds)."""
+    from oracle import rgf_oracle as O
+    from rgf_gb300 import gen
+    ns, nt, nd = w["ns"], w["nt"], w["nd"]
+
+    def run(k):
+        ia, ja, a = gen.generate_bta(ns, k, nd, w["seed"], spde_grid=w["spde"])
+        L = O.Layout(ns, k, nd)
+        t0 = time.perf_counter()
+        MF = O.ingest(L, ia, ja, a)
+        O.factorize(L, MF)
+        O.logdet(L, MF)
+        O.selinv_exact(L, MF)
+        dt = time.perf_counter() - t0
+        return O.algorithmic_flops(ns, k, nd)["total"], dt
+
+    k = min(nt, 2)
+    fl, dt = run(k)
+    per = dt / k
+    k2 = int(max(k, min(nt, target_s / max(per, 1e-9))))
+    if k2 > k:
+        fl, dt = run(k2)
+        k = k2
+    cores = os.cpu_count()
+    sample = f"ns={ns}, nt={k} of {nt}, nd={nd}: first {k} block columns, same generator"
+    return fl / dt / 1e12, cores, sample, dt
+
+
+def run_reference(args, w):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        tf, cores, sample, dt = cpu_port_sample(w, target_s=args.ref_seconds)
+        if i >= args.warmup:
+            vals.append((tf, dt))
+    tf = statistics.median(v[0] for v in vals)
+    ms = statistics.median(v[1] for v in vals) * 1e3
+    line = {"impl": "reference", "metric": METRIC, "value": tf, "unit": "TFLOP/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload, **cfg_of(w)},
+            "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cfg_of(w):
+    return {"ns": w["ns"], "nt": w["nt"], "nd": w["nd"], "seed": w["seed"],
+            "spde_grid": w["spde"], "parallelism": "replicas"}
+
+
+def run_rgf(args, w):
+    import torch
+    import rgf_gb300
+    from oracle import rgf_oracle as O
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.cuda.current_device()
+    ia, ja, a = make_inputs(w)
+    ns, nt, nd = w["ns"], w["nt"], w["nd"]
+    n = ns * nt + nd
+    flops = O.algorithmic_flops(ns, nt, nd)["total"]
+    # pinned host copies for the end-to-end leg
+    ia_p = torch.from_numpy(ia.view(np.int64)).pin_memory().numpy().view(np.uint64)
+    ja_p = torch.from_numpy(ja.view(np.int64)).pin_memory().numpy().view(np.uint64)
+    a_p = torch.from_numpy(a).pin_memory().numpy()
+    diag_host = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    del ia, ja, a
+
+    s = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
+                      slices=args.slices, device=dev)
+    stream = torch.cuda.ExternalStream(s.stream())
+
+    def step():
+        s.factorize()
+        s.logDet()
+        s.diag_device_ptr()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    k0 = s.info()["kernels_launched"]
+    s.kernel_timer(True)
+    s.kernel_timer_read(reset=True)
+    clocks = Clocks(dev)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_total = e0.elapsed_time(e1)
+    timer = s.kernel_timer_read(reset=True)
+    s.kernel_timer(False)
+    launches = s.info()["kernels_launched"] - k0
+    logdet = s.logDet()
+    if dist:
+        t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = flops * ws / (ms_step * 1e-3) / 1e12
+
+    # end-to-end through the public API: host CSC -> device, diag -> host
+    e2e_ms = []
+    for i in range(max(1, args.e2e_steps) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
+                          slices=args.slices, device=dev)
+        h.factorize()
+        h.logDet()
+        h.RGFdiag(diag_host)
+        h.close()
+        dt = (time.perf_counter() - t0) * 1e3
+        if i > 0:
+            e2e_ms.append(dt)
+    if dist:
+        t = torch.tensor([max(e2e_ms)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_med = float(t.item())
+    else:
+        e2e_med = statistics.median(e2e_ms)
+    h2d = ia_p.nbytes + ja_p.nbytes + a_p.nbytes
+    d2h = diag_host.nbytes + 8
+
+    # roofline of the dominant kernel: FP64 DMMA GEMM vs measured FP64 peak
+    peak = rgf_gb300.measure_fp64_peak()
+    per_launch_flops = timer["flops"] / max(1, timer["launches"])
+    per_launch_ms = timer["ms"] / max(1, timer["launches"])
+    achieved = per_launch_flops / (per_launch_ms * 1e-3) / 1e12 if timer["launches"] else None
+    roofline = {"bound": "tensor", "kernel": "gemm_fp64_kernel (DMMA m8n8k4)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if achieved else None, "traffic": None,
+                "peak_source": "FP64 DMMA m8n8k4 loop measured in this run (the peaks file "
+                               "has no FP64 figure)",
+                "kernel_share_of_step": timer["ms"] / ms_total if ms_total else None,
+                "launches_per_step": timer["launches"] / args.steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        tf, cores, sample, dt = cpu_port_sample(w, target_s=args.ref_seconds)
+        cpu = {"value": tf, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+               "sample": sample, "seconds": dt}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "bf16-slices/f64",
+                "data": "synthetic",
+                "config": {"workload": args.workload, **cfg_of(w), "precision": args.precision,
+                           "l2": "inputs larger than L2 (CSC %.1f GB, factor %.1f GB)" % (
+                               h2d / 1e9, s.info()["mf_size"] * 8 / 1e9)},
+                "e2e": {"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
+                        "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
+                "clocks": clk, "logdet": logdet,
+                "timed_region": "kernel timer on (events around each bulk GEMM launch), no graphs"}
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["rgf", "reference"], default="rgf")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="ns2000_nt100_nd6")
+    p.add_argument("--precision", choices=["fp64", "split"], default="fp64")
+    p.add_argument("--slices", type=int, default=0)
+    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--ref-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu", action="store_true")
+    args = p.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_rgf(args, w)
+
+
+if __name__ == "__main__":
+    main()

@@ -141,6 +141,10 @@ int rgf_kernel_timer_enable(rgf_handle* h, int enable);
 int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launches,
                           double* flops);
 
+/* Measured FP64 (DMMA m8n8k4) throughput of the current device in TFLOP/s:
+ * the denominator of the FP64 roofline.  Runs about 100 ms of GPU work. */
+int rgf_measure_fp64_peak(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

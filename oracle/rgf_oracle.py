@@ -203,7 +203,7 @@ def factorize(L: Layout, MF: np.ndarray) -> None:
         if prev is not None:
             Bm = prev[ns:2 * ns, :]                       # L_{i,i-1}
             D = P[:ns, :]
-            D[:, :] -= np.tril(Bm @ Bm.T)                 # RGF.H:276,304
+            D[:, :] -= np.tril(_blas.dsyrk(1.0, Bm, lower=1))   # RGF.H:276,304
             if nd:
                 ro_m = L.dense_row_offset(i - 1)
                 Cm = prev[ro_m:ro_m + nd, :]              # C_{i-1}

@@ -70,6 +70,7 @@ _SIGS = {
     "rgf_diag_device": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "rgf_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "rgf_kernel_timer_enable": (C.c_int, [C.c_void_p, C.c_int]),
+    "rgf_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "rgf_kernel_timer_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                         C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }
@@ -92,6 +93,14 @@ def load_library(path: str | None = None):
     if path is None:
         _LIB = lib
     return lib
+
+
+def measure_fp64_peak() -> float:
+    """FP64 (DMMA) TFLOP/s of the current GPU, measured by the library."""
+    lib = load_library()
+    out = C.c_double()
+    _check(lib.rgf_measure_fp64_peak(C.byref(out)), "rgf_measure_fp64_peak")
+    return out.value
 
 
 def _check(status: int, what: str) -> None:

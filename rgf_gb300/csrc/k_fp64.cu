@@ -277,3 +277,54 @@ void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const d
 }
 
 }  // namespace rgf
+
+// ---------------------------------------------------------------------------
+// FP64 peak probe: independent DMMA m8n8k4 chains on every SM, used as the
+// denominator of the FP64 roofline (the tensor-pipe FP64 rate of this GPU).
+// ---------------------------------------------------------------------------
+namespace rgf {
+namespace {
+__global__ void __launch_bounds__(256) dmma_peak_kernel(double* out, int iters) {
+  double a = 1.0 + threadIdx.x * 1e-9, b = 0.5;
+  double c[4][2] = {};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) dmma_8x8x4(c[j], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s += c[j][0] + c[j][1];
+  out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+int measure_fp64_peak(double* tflops) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 4;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 4;
+  const int blocks = sms * 8, threads = 256, iters = 1024;
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(double) * blocks * threads) != cudaSuccess) return 2;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    dmma_peak_kernel<<<blocks, threads>>>(buf, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (err != cudaSuccess) return 4;
+  const double flops = 2.0 * 8 * 8 * 4 * 4.0 * iters * (double)blocks * threads / 32.0;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return 0;
+}
+}  // namespace rgf

@@ -832,4 +832,9 @@ int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launc
   return RGF_OK;
 }
 
+int rgf_measure_fp64_peak(double* tflops) {
+  if (!tflops) return RGF_EINVAL;
+  return measure_fp64_peak(tflops);
+}
+
 }  // extern "C"

@@ -56,6 +56,9 @@ void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const d
                       long long ldl, int nbk, int mode, int batch, long long sX, long long sL,
                       cudaStream_t s);
 
+// Measured FP64 (DMMA) throughput of the current device in TFLOP/s.
+int measure_fp64_peak(double* tflops);
+
 // ---- small kernels (k_misc.cu) ------------------------------------------------
 struct BtaShape {
   long long ns, nt, nd, n;
