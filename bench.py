@@ -121,6 +121,7 @@ def cpu_port_sample(w, target_s: float = 12.0):
     Returns (tflops, cores, sample description, seconds)."""
     from oracle import rgf_oracle as O
     from rgf_gb300 import gen
+    from rgf_gb300.flops import algorithmic_flops
     ns, nt, nd = w["ns"], w["nt"], w["nd"]
 
     def run(k):
@@ -132,7 +133,7 @@ def cpu_port_sample(w, target_s: float = 12.0):
         O.logdet(L, MF)
         O.selinv_exact(L, MF)
         dt = time.perf_counter() - t0
-        return O.algorithmic_flops(ns, k, nd)["total"], dt
+        return algorithmic_flops(ns, k, nd)["total"], dt
 
     k = min(nt, 2)
     fl, dt = run(k)
@@ -176,7 +177,7 @@ def cfg_of(w):
 def run_rgf(args, w):
     import torch
     import rgf_gb300
-    from oracle import rgf_oracle as O
+    from rgf_gb300.flops import algorithmic_flops
 
     ws, rank, local = dist_env()
     dist = None
@@ -188,7 +189,7 @@ def run_rgf(args, w):
     ia, ja, a = make_inputs(w)
     ns, nt, nd = w["ns"], w["nt"], w["nd"]
     n = ns * nt + nd
-    flops = O.algorithmic_flops(ns, nt, nd)["total"]
+    flops = algorithmic_flops(ns, nt, nd)["total"]
     # pinned host copies for the end-to-end leg
     ia_p = torch.from_numpy(ia.view(np.int64)).pin_memory().numpy().view(np.uint64)
     ja_p = torch.from_numpy(ja.view(np.int64)).pin_memory().numpy().view(np.uint64)
@@ -239,7 +240,7 @@ def run_rgf(args, w):
 
     # end-to-end through the public API: host CSC -> device, diag -> host
     e2e_ms = []
-    for i in range(max(1, args.e2e_steps) + 1):
+    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
@@ -251,12 +252,11 @@ def run_rgf(args, w):
         dt = (time.perf_counter() - t0) * 1e3
         if i > 0:
             e2e_ms.append(dt)
-    if dist:
+    e2e_med = statistics.median(e2e_ms) if e2e_ms else float("nan")
+    if dist and e2e_ms:
         t = torch.tensor([max(e2e_ms)], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_med = float(t.item())
-    else:
-        e2e_med = statistics.median(e2e_ms)
     h2d = ia_p.nbytes + ja_p.nbytes + a_p.nbytes
     d2h = diag_host.nbytes + 8
 
@@ -287,9 +287,9 @@ def run_rgf(args, w):
                 "config": {"workload": args.workload, **cfg_of(w), "precision": args.precision,
                            "l2": "inputs larger than L2 (CSC %.1f GB, factor %.1f GB)" % (
                                h2d / 1e9, s.info()["mf_size"] * 8 / 1e9)},
-                "e2e": {"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
-                        "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h},
+                "e2e": ({"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
+                         "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
                 "clocks": clk, "logdet": logdet,
                 "timed_region": "kernel timer on (events around each bulk GEMM launch), no graphs"}

@@ -1,0 +1,109 @@
+/*
+ * RGF.H -- drop-in C++ class for the reference's RGF<double> (RGF.H:11-80),
+ * implemented over the C ABI of librgf_gb300 (rgf.h).
+ *
+ * Same class name, constructor and method signatures as the reference, so a
+ * program written against the reference (its driver main.C included)
+ * compiles unchanged with -I<this dir> and links with -lrgf_gb300.
+ * Differences, all behaviour-compatible:
+ *   - the CSC arrays are copied to the GPU at construction (the pointers are
+ *     still kept, as in the reference, but no longer read after it);
+ *   - the factor stays resident on the GPU; RGFdiag does not invalidate it;
+ *   - errors throw std::runtime_error instead of being ignored;
+ *   - RGFdiag returns the exact diag(A^{-1}).  Set RGF_GB300_SELINV=compat to
+ *     get the reference's recursion instead, RGF_GB300_PRECISION=split for
+ *     the split-precision path.
+ * Only T = double is provided (the reference's driver uses double, main.C:13-16).
+ */
+#ifndef RGF_GB300_DROPIN_RGF_H
+#define RGF_GB300_DROPIN_RGF_H
+
+#include <sys/time.h>
+
+#include <cstddef>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "rgf.h"
+
+/* Wall-clock helper of the reference's Utilities.C (main.C times with it). */
+inline double get_time(double t0) {
+  timeval tim;
+  gettimeofday(&tim, NULL);
+  return (double)(tim.tv_sec + (tim.tv_usec / 1000000.0)) - t0;
+}
+
+template <class T>
+class RGF;
+
+template <>
+class RGF<double> {
+ public:
+  RGF(size_t* ia, size_t* ja, double* a, size_t ns, size_t nt, size_t nd)
+      : ia_(ia), ja_(ja), a_(a), n_(ns * nt + nd), h_(NULL) {
+    rgf_opts o;
+    rgf_default_opts(&o);
+    const char* sel = std::getenv("RGF_GB300_SELINV");
+    if (sel && std::strcmp(sel, "compat") == 0) o.selinv_mode = RGF_SELINV_COMPAT;
+    const char* prec = std::getenv("RGF_GB300_PRECISION");
+    if (prec && std::strcmp(prec, "split") == 0) o.precision = RGF_PREC_SPLIT;
+    check(rgf_create(ia, ja, a, ns, nt, nd, &o, &h_), "RGF::RGF");
+  }
+
+  RGF(size_t* ia, size_t* ja, double* a, size_t ns, size_t nt, size_t nd, const rgf_opts& o)
+      : ia_(ia), ja_(ja), a_(a), n_(ns * nt + nd), h_(NULL) {
+    check(rgf_create(ia, ja, a, ns, nt, nd, &o, &h_), "RGF::RGF");
+  }
+
+  ~RGF() {
+    if (h_) rgf_destroy(h_);
+  }
+
+  void factorize() { check(rgf_factorize(h_), "RGF::factorize"); }
+
+  void solve(double* b, size_t nrhs) { solve(b, b, nrhs); }
+
+  void solve(double* x, double* b, size_t nrhs) {
+    check(rgf_solve(h_, x, b, nrhs), "RGF::solve");
+  }
+
+  void RGFdiag(double* diag) { check(rgf_diag(h_, diag), "RGF::RGFdiag"); }
+
+  double logDet() {
+    double v = 0.0;
+    check(rgf_logdet(h_, &v), "RGF::logDet");
+    return v;
+  }
+
+  double residualNorm(double* x, double* b) {
+    double v = 0.0;
+    check(rgf_residual_norm(h_, x, b, &v), "RGF::residualNorm");
+    return v;
+  }
+
+  double residualNormNormalized(double* x, double* b) {
+    double v = 0.0;
+    check(rgf_residual_norm_normalized(h_, x, b, &v), "RGF::residualNormNormalized");
+    return v;
+  }
+
+  rgf_handle* handle() { return h_; }
+
+ private:
+  RGF(const RGF&);
+  RGF& operator=(const RGF&);
+
+  static void check(int status, const char* what) {
+    if (status != RGF_OK) throw std::runtime_error(std::string(what) + ": " + rgf_status_string(status));
+  }
+
+  size_t* ia_;
+  size_t* ja_;
+  double* a_;
+  size_t n_;
+  rgf_handle* h_;
+};
+
+#endif /* RGF_GB300_DROPIN_RGF_H */

@@ -433,28 +433,3 @@ def run_all(ns, nt, nd, ia, ja, a, b=None, exact=True) -> dict:
         out["x"] = solve(L, MF, b)
     out["diag"] = selinv_exact(L, MF) if exact else selinv_compat(L, MF)
     return out
-
-
-def algorithmic_flops(ns: int, nt: int, nd: int) -> dict:
-    """LAPACK-convention flop counts of factorize and selected inversion.
-
-    Per block column i with b = ns, d = nd:
-      factor: b^3/3 + (b [i<nt-1] + d) b^2 + [i<nt-1](b^2(b+1) + 2 d b^2) + d^2 (b+1)
-              plus d^3/3 once (corner POTRF);
-      selinv: b^3/3 + 2 b^3 + [i<nt-1] 4 b^3 + 2 d^2 b + 2 d b^2 + [i<nt-1] 4 d b^2
-              plus 4 d^3/3 once.
-    """
-    b, d = float(ns), float(nd)
-    fac = sel = 0.0
-    for i in range(nt):
-        last = i == nt - 1
-        fac += b ** 3 / 3 + ((0 if last else b) + d) * b * b
-        if not last:
-            fac += b * b * (b + 1) + 2 * d * b * b
-        fac += d * d * (b + 1)
-        sel += b ** 3 / 3 + 2 * b ** 3 + 2 * d * d * b + 2 * d * b * b
-        if not last:
-            sel += 4 * b ** 3 + 4 * d * b * b
-    fac += d ** 3 / 3
-    sel += 4 * d ** 3 / 3
-    return {"factor": fac, "selinv": sel, "total": fac + sel}

@@ -17,6 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librgf_gb300.so")
+CLI = os.path.join(HERE, "rgf_main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
@@ -68,7 +69,23 @@ def build(verbose: bool = False, extra=()) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """The main.C-compatible command-line driver, linked against the library."""
+    src = os.path.join(HERE, "cli", "rgf_main.cpp")
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(src),
+                                                            os.path.getmtime(LIB)):
+        return CLI
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", CLI,
+           "-L", HERE, "-lrgf_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"rgf_main build failed:\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,0 +1,80 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports
+every entry point include/rgf.h declares; the generator, .dat I/O and flop
+counts behave as documented."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_entry_points():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(rgf_\w+)\s*\(", src, re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    import rgf_gb300
+    lib = rgf_gb300.load_library()
+    names = declared_entry_points()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(lib, n), n
+    # a status string call needs no device
+    lib.rgf_status_string.restype = ctypes.c_char_p
+    assert lib.rgf_status_string(3).startswith(b"RGF_ENOTSPD")
+
+
+def test_missing_device_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import rgf_gb300
+    from rgf_gb300 import gen
+    ia, ja, a = gen.generate_bta(3, 3, 2, 1)
+    with pytest.raises(rgf_gb300.RGFError) as e:
+        rgf_gb300.RGF(ia, ja, a, 3, 3, 2)
+    assert e.value.status == 4
+
+
+def test_generator_is_seeded_and_spd():
+    from oracle import rgf_oracle as O
+    from rgf_gb300 import gen
+    a1 = gen.generate_bta(6, 4, 2, 9)
+    a2 = gen.generate_bta(6, 4, 2, 9)
+    for x, y in zip(a1, a2):
+        assert np.array_equal(x, y)
+    ia, ja, a = a1
+    assert len(ja) == gen.bta_nnz(6, 4, 2)
+    A = O.to_dense(ia, ja, a)
+    assert np.all(np.linalg.eigvalsh(A) > 0)
+    # lower CSC, sorted rows, diagonal first
+    for c in range(len(ia) - 1):
+        rows = ja[ia[c]:ia[c + 1]].astype(int)
+        assert rows[0] == c and np.all(np.diff(rows) > 0)
+
+
+def test_dat_round_trip(tmp_path):
+    from rgf_gb300 import gen
+    ia, ja, a = gen.generate_bta(4, 3, 1, 2)
+    p = tmp_path / "m.dat"
+    gen.write_dat(p, ia, ja, a)
+    n, ia2, ja2, a2 = gen.read_dat(p)
+    assert n == len(ia) - 1
+    assert np.array_equal(ia, ia2) and np.array_equal(ja, ja2) and np.array_equal(a, a2)
+
+
+def test_flop_contract():
+    from rgf_gb300.flops import algorithmic_flops
+    f = algorithmic_flops(2000, 100, 6)
+    assert abs(f["factor"] - 1.858e12) / 1.858e12 < 1e-3
+    assert abs(f["selinv"] - 5.049e12) / 5.049e12 < 1e-3
+    f = algorithmic_flops(1000, 50, 4)
+    assert abs(f["total"] - 4.292e11) / 4.292e11 < 1e-3
