@@ -145,6 +145,31 @@ int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launc
  * the denominator of the FP64 roofline.  Runs about 100 ms of GPU work. */
 int rgf_measure_fp64_peak(double* tflops);
 
+/* Largest n accepted by rgf_residual_norm_noalloc (8 MiB of doubles). */
+#define RGF_NOALLOC_MAX_N ((size_t)1 << 20)
+
+/* Allocation-free residual: d_out[0] = ||b - A x||_2, d_out[1] = ||b||_2 for
+ * the symmetric matrix given by its lower CSC (n+1 column pointers d_ia, row
+ * indices d_ja, values d_a), first right-hand side only.  Every pointer is
+ * DEVICE memory on the current device and the work is queued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream); read d_out after that
+ * stream has finished.
+ * This entry point has no counterpart in the reference.  It exists for
+ * callers that cannot call cudaMalloc: frameworks whose allocator already
+ * holds nearly all device memory, serving loops that keep cudaMalloc and
+ * cudaFree (which waits for the whole device) out of their steady state, and
+ * embeddings that forbid hidden allocations.  It allocates nothing: its
+ * scratch (n doubles) is a fixed 8 MiB device array that every GPU loading
+ * this library holds until the process exits, so n must not exceed
+ * RGF_NOALLOC_MAX_N (RGF_EINVAL otherwise).  The first call on a device looks
+ * up that array's device address (once per device, with the device current);
+ * make that first call before any stream capture.  All calls share the array:
+ * calls whose work overlaps on the GPU race and give wrong results, so
+ * serialize them (one stream, or events). */
+int rgf_residual_norm_noalloc(size_t n, const size_t* d_ia, const size_t* d_ja,
+                              const double* d_a, const double* d_x, const double* d_b,
+                              double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     import rgf_gb300
     lib = rgf_gb300.load_library()
     names = declared_entry_points()
-    assert len(names) >= 18
+    assert len(names) >= 19
     for n in names:
         assert hasattr(lib, n), n
     # a status string call needs no device
