@@ -39,6 +39,8 @@ WORKLOADS = {
     "ns2000_nt100_nd6": dict(ns=2000, nt=100, nd=6, seed=3, spde=None),
     "ns1000_nt50_nd4": dict(ns=1000, nt=50, nd=4, seed=2, spde=(40, 25)),
     "ns3_nt3_nd2": dict(ns=3, nt=3, nd=2, seed=1, spde=None),
+    # a 20-block prefix of the default workload, for profiling runs
+    "ns2000_nt20_nd6": dict(ns=2000, nt=20, nd=6, seed=3, spde=None),
 }
 METRIC = "FP64-equiv TFLOP/s for factorize+logDet+RGFdiag"
 

@@ -51,7 +51,10 @@ typedef struct rgf_opts {
   int selinv_mode;  /* enum rgf_selinv_mode (default RGF_SELINV_EXACT)        */
   int device;       /* CUDA device ordinal, -1 = the current device           */
   int use_graphs;   /* 1 = replay each stage as a captured CUDA graph         */
-  int reserved[11];
+  int fp64_diag;    /* split precision: 1 (default) keeps the Cholesky and the
+                       inverse of every diagonal block entirely in FP64; 0 runs
+                       their large inner updates as split products too        */
+  int reserved[10];
 } rgf_opts;
 
 typedef struct rgf_handle rgf_handle;
@@ -140,6 +143,16 @@ int rgf_get_stream(rgf_handle* h, void** stream);
 int rgf_kernel_timer_enable(rgf_handle* h, int enable);
 int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launches,
                           double* flops);
+
+/* C := alpha op(A) op(B) + beta C on device memory (column-major, BLAS
+ * argument conventions, transa/transb 'N' or 'T'), queued on `stream` and
+ * completed before return.  precision RGF_PREC_FP64 runs the FP64 DMMA
+ * kernel; RGF_PREC_SPLIT runs the split-precision tensor-core kernel with
+ * `slices` bf16 digits per operand (0 = default) when k is large enough, else
+ * FP64.  These are the kernels of the solver's bulk updates. */
+int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m, int n, int k,
+                     double alpha, const double* A, int lda, const double* B, int ldb,
+                     double beta, double* C, int ldc, void* stream);
 
 /* Measured FP64 (DMMA m8n8k4) throughput of the current device in TFLOP/s:
  * the denominator of the FP64 roofline.  Runs about 100 ms of GPU work. */

@@ -37,7 +37,8 @@ class RGFError(RuntimeError):
 
 class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("slices", C.c_int), ("selinv_mode", C.c_int),
-                ("device", C.c_int), ("use_graphs", C.c_int), ("reserved", C.c_int * 11)]
+                ("device", C.c_int), ("use_graphs", C.c_int), ("fp64_diag", C.c_int),
+                ("reserved", C.c_int * 10)]
 
 
 class _Info(C.Structure):
@@ -71,6 +72,9 @@ _SIGS = {
     "rgf_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "rgf_kernel_timer_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "rgf_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "rgf_dgemm_device": (C.c_int, [C.c_int, C.c_int, C.c_char, C.c_char, C.c_int, C.c_int,
+                                   C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p,
+                                   C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
     "rgf_kernel_timer_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                         C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }
@@ -103,6 +107,17 @@ def measure_fp64_peak() -> float:
     return out.value
 
 
+def dgemm_device(precision: str, transa: str, transb: str, m: int, n: int, k: int,
+                 alpha: float, A_ptr: int, lda: int, B_ptr: int, ldb: int, beta: float,
+                 C_ptr: int, ldc: int, stream: int = 0, slices: int = 0) -> None:
+    """C := alpha op(A) op(B) + beta C on device pointers (column-major)."""
+    lib = load_library()
+    _check(lib.rgf_dgemm_device(PRECISION[precision], int(slices), transa.encode(),
+                                transb.encode(), m, n, k, alpha, C.c_void_p(A_ptr), lda,
+                                C.c_void_p(B_ptr), ldb, beta, C.c_void_p(C_ptr), ldc,
+                                C.c_void_p(stream)), "rgf_dgemm_device")
+
+
 def _check(status: int, what: str) -> None:
     if status != 0:
         raise RGFError(status, what)
@@ -122,7 +137,7 @@ class RGF:
 
     def __init__(self, ia, ja, a, ns: int, nt: int, nd: int, precision: str = "fp64",
                  slices: int = 0, selinv: str = "exact", device: int = -1,
-                 use_graphs: bool = True):
+                 use_graphs: bool = True, fp64_diag: bool = True):
         lib = load_library()
         self._lib = lib
         self._h = C.c_void_p()
@@ -143,6 +158,7 @@ class RGF:
         o.selinv_mode = SELINV[selinv]
         o.device = int(device)
         o.use_graphs = 1 if use_graphs else 0
+        o.fp64_diag = 1 if fp64_diag else 0
         _check(lib.rgf_create(_ptr(self._ia), _ptr(self._ja), _ptr(self._a), self.ns, self.nt,
                               self.nd, C.byref(o), C.byref(self._h)), "rgf_create")
 

@@ -142,48 +142,74 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
 
 // ---------------------------------------------------------------------------
 // Leaf Cholesky of one <= 64 x 64 diagonal tile, right-looking in shared memory.
+// GB300's FP64 pipe retires about two lanes per cycle per SM, so every FP64
+// warp instruction is expensive: the pivot's reciprocal square root is formed
+// once per column by one warp (an FP32 seed refined by two Newton steps), the
+// trailing update maps warps to columns and lanes to rows (no index
+// arithmetic per element), and the tile's 64 logs run in parallel.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) leaf_potrf_kernel(double* T, long long ldt, int nbk,
+__device__ __forceinline__ double rsqrt_newton(double d) {
+  // d > 0 and normal: d = m * 4^k with m in [1, 4)
+  const long long b = __double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e == -1023) return 1.0 / sqrt(d);  // subnormal pivot
+  const int k = e >> 1;
+  const double m = __longlong_as_double(b - ((long long)(2 * k) << 52));
+  double y = (double)rsqrtf((float)m);
+  const double hm = 0.5 * m;
+  y = y * fma(-hm, y * y, 1.5);
+  y = y * fma(-hm, y * y, 1.5);
+  return y * __longlong_as_double((long long)(1023 - k) << 52);
+}
+
+__global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ldt, int nbk,
                                                          int col0, double* logpart,
                                                          DevStatus* st) {
   __shared__ double S[64][65];
+  __shared__ double piv[2];
+  __shared__ double lg[64];
   __shared__ int fail;
-  const int tid = threadIdx.x;
-  for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
-    const int c = idx / nbk, r = idx % nbk;
-    S[r][c] = (r >= c) ? T[(long long)r + (long long)c * ldt] : 0.0;
-  }
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+  for (int c = warp; c < nbk; c += nw)
+    for (int r = lane; r < nbk; r += 32)
+      S[r][c] = (r >= c) ? T[(long long)r + (long long)c * ldt] : 0.0;
   if (tid == 0) fail = -1;
   __syncthreads();
   for (int j = 0; j < nbk; ++j) {
-    if (tid == 0) {
-      double d = S[j][j];
-      if (!(d > 0.0)) {
-        if (fail < 0) fail = j;
-        d = __longlong_as_double(0x7ff8000000000000LL);  // NaN marks the failed pivot
+    if (warp == 0) {
+      const double d = S[j][j];
+      const bool ok = d > 0.0;
+      const double y = rsqrt_newton(ok ? d : 1.0);
+      if (lane == 0) {
+        if (!ok && fail < 0) fail = j;
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        piv[0] = ok ? d * y : nan;  // L_jj
+        piv[1] = ok ? y : nan;      // 1 / L_jj
       }
-      S[j][j] = sqrt(d);
     }
     __syncthreads();
-    const double rinv = 1.0 / S[j][j];
+    const double rinv = piv[1];
     for (int r = j + 1 + tid; r < nbk; r += blockDim.x) S[r][j] *= rinv;
+    if (tid == 0) S[j][j] = piv[0];
     __syncthreads();
-    const int m = nbk - j - 1;
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
-      const int c = idx / m, r = idx % m;
-      if (r >= c) S[j + 1 + r][j + 1 + c] -= S[j + 1 + r][j] * S[j + 1 + c][j];
+    for (int c = j + 1 + warp; c < nbk; c += nw) {
+      const double ljc = S[c][j];
+      for (int r = c + lane; r < nbk; r += 32) S[r][c] = fma(-S[r][j], ljc, S[r][c]);
     }
     __syncthreads();
   }
-  for (int idx = tid; idx < nbk * nbk; idx += blockDim.x) {
-    const int c = idx / nbk, r = idx % nbk;
-    if (r >= c) T[(long long)r + (long long)c * ldt] = S[r][c];
-  }
-  if (tid == 0) {
-    double s = 0.0;
-    for (int j = 0; j < nbk; ++j) s += log(S[j][j]);
-    *logpart = s;
-    if (fail >= 0) atomicMin(&st->not_spd_col, col0 + fail);
+  for (int c = warp; c < nbk; c += nw)
+    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c];
+  if (tid < nbk) lg[tid] = log(S[tid][tid]);
+  __syncthreads();
+  if (warp == 0) {
+    double v = (lane < nbk ? lg[lane] : 0.0) + (lane + 32 < nbk ? lg[lane + 32] : 0.0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      *logpart = v;
+      if (fail >= 0) atomicMin(&st->not_spd_col, col0 + fail);
+    }
   }
 }
 
@@ -192,7 +218,7 @@ __global__ void __launch_bounds__(128) leaf_potrf_kernel(double* T, long long ld
 // owns one row of X in registers; the tile is broadcast from shared memory.
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs, long long xcs,
+__global__ void __launch_bounds__(32) trsm_rows_kernel(double* X, long long xrs, long long xcs,
                                                         int rows, const double* L, long long ldl,
                                                         int nbk, long long sX, long long sL) {
   __shared__ double Ls[64][65];
@@ -206,10 +232,7 @@ __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs
     Ls[r][c] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 64) {
-    const int j = threadIdx.x;
-    rinv[j] = (j < nbk) ? 1.0 / Ls[j][j] : 0.0;
-  }
+  for (int j = threadIdx.x; j < 64; j += blockDim.x) rinv[j] = (j < nbk) ? 1.0 / Ls[j][j] : 0.0;
   __syncthreads();
   const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
@@ -262,18 +285,18 @@ void launch_gemm_fp64(const GemmDesc& g, cudaStream_t s) {
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, double* logpart,
                        DevStatus* st, cudaStream_t s) {
   if (nbk <= 0) return;
-  leaf_potrf_kernel<<<1, 128, 0, s>>>(T, ldt, nbk, col0, logpart, st);
+  leaf_potrf_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, logpart, st);
 }
 
 void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,
                       long long ldl, int nbk, int mode, int batch, long long sX, long long sL,
                       cudaStream_t s) {
   if (rows <= 0 || nbk <= 0 || batch <= 0) return;
-  dim3 grid((rows + 127) / 128, batch);
+  dim3 grid((rows + 31) / 32, batch);
   if (mode == 0)
-    trsm_rows_kernel<0><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+    trsm_rows_kernel<0><<<grid, 32, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
   else
-    trsm_rows_kernel<1><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+    trsm_rows_kernel<1><<<grid, 32, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
 }
 
 }  // namespace rgf

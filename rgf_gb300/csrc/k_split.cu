@@ -1,20 +1,617 @@
-// Split-precision GEMM engine (not available in this build yet).
+// Split-precision GEMM engine (Ozaki scheme) on the tcgen05 tensor cores.
+//
+// D = alpha * op(A) * op(B) + beta * C with FP64 operands:
+//  1. every row r of op(A) is scaled by 2^-ea[r] (|x| < 2^ea[r]) and cut into
+//     S base-2^beta digits (integers |d| < 2^beta, exact in bf16); every column
+//     c of op(B) likewise with 2^-eb[c].  The cut is done on the FP64 bit
+//     pattern with integer instructions only (no FP64 arithmetic).
+//  2. for every digit pair (s, t) with s + t <= S + 1 the tensor cores form
+//     the integer products P_st = A_s B_t, 1024 terms at a time, in FP32 in
+//     tensor memory; with beta = 7 each 1024-term sum is below 2^24 and thus
+//     exact.
+//  3. each exact partial is moved to registers and added, shifted by its
+//     level, into a 64-bit integer fixed-point accumulator;
+//  4. one conversion to FP64 per output, scaled by 2^(ea[r] + eb[c] + ...).
+// The GEMM kernel is warp specialized: one warp issues TMA tile loads
+// (cp.async.bulk.tensor, 128B swizzle) into a 4-stage shared-memory ring, one
+// elected thread issues tcgen05.mma (M=128, N=128, K=16, bf16 -> f32) into
+// two TMEM accumulators, and eight warps drain the accumulators while the next
+// product accumulates.  Every wait on an mbarrier is bounded; a wait that
+// gives up records a timeout in the device status word and the CTA exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
 #include "../../include/rgf.h"
 #include "rgf_split.h"
 
 namespace rgf {
 
-SplitEngine* SplitEngine::create(int slices, int* status) {
-  (void)slices;
-  *status = RGF_ENOTSUP;
-  return nullptr;
+namespace {
+
+constexpr int BM = 128, BN = 128, BKE = 64;  // tile rows, cols, K elements per stage
+constexpr int NSTAGE = 4;
+constexpr int KCHUNK_BLOCKS = 16;             // 16 x 64 = 1024 terms per exact FP32 sum
+constexpr int SPLIT_BETA = 7;
+constexpr int MAXPAIRS = 45;
+constexpr int NUM_THREADS = 320;              // warp 0 TMA, warp 1 MMA, warps 2..9 drain
+constexpr uint32_t TILE_BYTES = BM * BKE * 2; // 16 KiB per operand tile
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any mbarrier wait
+
+struct SplitParams {
+  int m, n, k;
+  int S, beta, cs;
+  int npairs;
+  unsigned char ps[MAXPAIRS], pt[MAXPAIRS];
+  int triA, triB, outLower;
+  const int* exA;
+  const int* exB;
+  const double* C;
+  long long ldc;
+  double* D;
+  long long ldd;
+  double alpha, betac;
+  DevStatus* st;
+};
+
+// ---- PTX wrappers -----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-SplitEngine::~SplitEngine() = default;
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
 
-long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s) {
-  launch_gemm_fp64(g, s);
-  return 1;
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after WAIT_NS of wall time (or when another role of
+// the CTA already gave up), raises the CTA abort flag, records a timeout in
+// the device status word and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          DevStatus* st) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (long long it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if ((it & 255) == 0 && global_ns() - t0 > WAIT_NS) break;
+  }
+  *abort_flag = 1;
+  atomicExch(&st->timeout, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// K-major operand tile: 128 rows of 128 bytes, 128B swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void* base) {
+  uint64_t d = 0;
+  d |= (uint64_t)((smem_u32(base) >> 4) & 0x3FFF);       // start address
+  d |= (uint64_t)1 << 16;                                 // leading byte offset (unused)
+  d |= (uint64_t)(1024 >> 4) << 32;                       // stride byte offset
+  d |= (uint64_t)1 << 46;                                 // descriptor version
+  d |= (uint64_t)2 << 61;                                 // 128B swizzle
+  return d;
+}
+
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M=128, N=128.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ double pow2(int e) {
+  if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
+  return ldexp(1.0, e);
+}
+
+// Per-tile K range: triangular operands have no terms outside their triangle.
+__device__ __forceinline__ void tile_kblocks(const SplitParams& p, int m0, int n0, int& kb_lo,
+                                             int& kb_hi) {
+  int lo = 0, hi = p.k;
+  if (p.triA == TRI_LOWER) hi = min(hi, m0 + BM);
+  if (p.triA == TRI_UPPER) lo = max(lo, m0);
+  if (p.triB == TRI_LOWER) lo = max(lo, n0);
+  if (p.triB == TRI_UPPER) hi = min(hi, n0 + BN);
+  kb_lo = lo / BKE;
+  kb_hi = hi > lo ? (hi + BKE - 1) / BKE : kb_lo;
+}
+
+// ---- the slice-product GEMM ---------------------------------------------------
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    split_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                      const __grid_constant__ CUtensorMap tmB, const __grid_constant__ SplitParams p) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint8_t* tilesA = smem;                                  // NSTAGE x 16 KiB
+  uint8_t* tilesB = smem + NSTAGE * TILE_BYTES;            // NSTAGE x 16 KiB
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 2 * NSTAGE * TILE_BYTES);
+  uint64_t* empty = full + NSTAGE;
+  uint64_t* acc_full = empty + NSTAGE;                     // 2 accumulators
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  if (p.outLower && m0 + BM <= n0) return;  // whole tile above the diagonal (uniform exit)
+
+  int kb_lo, kb_hi;
+  tile_kblocks(p, m0, n0, kb_lo, kb_hi);
+  const int nkb = kb_hi - kb_lo;
+  const int nchunks = (nkb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
+  const int njobs = nchunks * p.npairs;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 8);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {  // allocate 256 TMEM columns (two 128-column accumulators)
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      long long use = 0;
+      for (int j = 0; j < njobs && !*abort_flag; ++j) {
+        const int c = j / p.npairs, pr = j % p.npairs;
+        const int kb0 = kb_lo + c * KCHUNK_BLOCKS, kb1 = min(kb_hi, kb0 + KCHUNK_BLOCKS);
+        for (int kb = kb0; kb < kb1; ++kb, ++use) {
+          const int s = (int)(use % NSTAGE);
+          const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
+          if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, p.st)) break;
+          mbar_expect_tx(&full[s], 2 * TILE_BYTES);
+          tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], kb * BKE, m0, p.ps[pr]);
+          tma_load_3d(tilesB + s * TILE_BYTES, &tmB, &full[s], kb * BKE, n0, p.pt[pr]);
+        }
+      }
+      // let in-flight loads land before the CTA can exit
+      if (use > 0) {
+        const long long last = use - 1;
+        mbar_wait(&full[last % NSTAGE], (uint32_t)((last / NSTAGE) & 1), abort_flag, p.st);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      long long use = 0;
+      for (int j = 0; j < njobs && !*abort_flag; ++j) {
+        const int buf = j & 1;
+        const uint32_t aph = (uint32_t)((j >> 1) & 1);
+        if (!mbar_wait(&acc_empty[buf], aph ^ 1u, abort_flag, p.st)) break;
+        tc_fence_after();
+        const uint32_t tacc = tmem_base + (uint32_t)(buf * BN);
+        const int c = j / p.npairs;
+        const int kb0 = kb_lo + c * KCHUNK_BLOCKS, kb1 = min(kb_hi, kb0 + KCHUNK_BLOCKS);
+        bool ok = true;
+        for (int kb = kb0; kb < kb1; ++kb, ++use) {
+          const int s = (int)(use % NSTAGE);
+          const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
+          if (!mbar_wait(&full[s], ph, abort_flag, p.st)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t ad = smem_desc_sw128(tilesA + s * TILE_BYTES);
+          const uint64_t bd = smem_desc_sw128(tilesB + s * TILE_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < BKE / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle atom
+            umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2),
+                      (kb > kb0 || kk > 0) ? 1u : 0u);
+          umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+        }
+        if (!ok) break;
+        umma_commit(&acc_full[buf]);  // accumulator ready for the drain warps
+      }
+      // wait for the last commit so no MMA is in flight at exit
+      if (njobs > 0 && !*abort_flag) {
+        const int j = njobs - 1;
+        mbar_wait(&acc_full[j & 1], (uint32_t)((j >> 1) & 1), abort_flag, p.st);
+      }
+    }
+  } else {
+    // ---------------- drain warps (2..9) ----------------
+    const int q = warp & 3;            // TMEM lane quadrant this warp may access
+    const int half = (warp - 2) >> 2;  // column half: 0 or 1
+    const int row = q * 32 + lane;     // accumulator row of this thread
+    long long acc[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) acc[i] = 0;
+    for (int j = 0; j < njobs; ++j) {
+      const int buf = j & 1;
+      if (!mbar_wait(&acc_full[buf], (uint32_t)((j >> 1) & 1), abort_flag, p.st)) break;
+      tc_fence_after();
+      const int pr = j % p.npairs;
+      const int level = p.ps[pr] + p.pt[pr] + 2;
+      const int sh = p.beta * (p.S + 1 - level) - p.cs;
+      const uint32_t taddr =
+          tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + half * 64);
+#pragma unroll
+      for (int part = 0; part < 4; ++part) {
+        uint32_t r[16];
+        tmem_ld16(taddr + part * 16, r);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const long long v = (long long)__float2int_rn(__uint_as_float(r[i]));
+          acc[part * 16 + i] += sh >= 0 ? (v << sh) : (v >> (-sh));
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
+    }
+    // epilogue: one FP64 conversion per output
+    const int r = m0 + row;
+    if (r < p.m && !*abort_flag) {
+      const int er = p.exA[r] + p.cs - p.beta * (p.S + 1);
+      const int cbase = n0 + half * 64;
+#pragma unroll
+      for (int i = 0; i < 64; ++i) {
+        const int c = cbase + i;
+        if (c < p.n && !(p.outLower && r < c)) {
+          double v = p.alpha * ((double)acc[i] * pow2(er + p.exB[c]));
+          if (p.betac != 0.0) v += p.betac * p.C[(long long)r + (long long)c * p.ldc];
+          p.D[(long long)r + (long long)c * p.ldd] = v;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem_base)
+                 : "memory");
+  }
+}
+
+// ---- slicing ------------------------------------------------------------------
+// X is R x K with element (r, k) at X[r*rs + k*ks]; tri masks op(X)'s other
+// triangle.  ex[r] = smallest e with |x| < 2^e over the row (0 for a zero row).
+__device__ __forceinline__ bool tri_ok(int tri, int r, int k) {
+  return tri == TRI_NONE || (tri == TRI_LOWER ? k <= r : k >= r);
+}
+
+__device__ __forceinline__ int exp_of_max(unsigned long long mx) {
+  if (mx == 0) return 0;
+  const int E = (int)((mx >> 52) & 0x7ff);
+  return (E == 0 ? -1022 : E - 1023) + 1;
+}
+
+// one thread per row, rows contiguous (rs == 1): coalesced across the warp
+__global__ void row_exp_rowmajor_kernel(const double* X, long long ks, int R, int K, int tri,
+                                        int* ex, int Rp) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= Rp) return;
+  unsigned long long mx = 0;
+  if (r < R)
+    for (int k = 0; k < K; ++k)
+      if (tri_ok(tri, r, k)) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong(X[r + (long long)k * ks]) &
+            0x7fffffffffffffffull;
+        mx = b > mx ? b : mx;
+      }
+  ex[r] = exp_of_max(mx);
+}
+
+// one warp per row, k contiguous (ks == 1)
+__global__ void row_exp_kmajor_kernel(const double* X, long long rs, int R, int K, int tri,
+                                      int* ex, int Rp) {
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (r >= Rp) return;
+  unsigned long long mx = 0;
+  if (r < R)
+    for (int k = lane; k < K; k += 32)
+      if (tri_ok(tri, r, k)) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong(X[(long long)r * rs + k]) &
+            0x7fffffffffffffffull;
+        mx = b > mx ? b : mx;
+      }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = y > mx ? y : mx;
+  }
+  if (lane == 0) ex[r] = exp_of_max(mx);
+}
+
+// 32 x 32 tiles through shared memory: read coalesced along the contiguous
+// dimension, write the S digit planes coalesced along k.
+__global__ void slice_kernel(const double* X, long long rs, long long ks, int R, int K, int tri,
+                             const int* ex, __nv_bfloat16* out, int Rp, int Kp, int S, int beta) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int rl, kl;
+    if (rs == 1) { rl = tx; kl = ty + 8 * i; }
+    else         { kl = tx; rl = ty + 8 * i; }
+    const int r = r0 + rl, k = k0 + kl;
+    double v = 0.0;
+    if (r < R && k < K && tri_ok(tri, r, k)) v = X[(long long)r * rs + (long long)k * ks];
+    tile[rl][kl] = v;
+  }
+  __syncthreads();
+  const unsigned long long dmask = (1ull << beta) - 1ull;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int rl = ty + 8 * i, r = r0 + rl, k = k0 + tx;
+    if (r >= Rp || k >= Kp) continue;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(tile[rl][tx]);
+    const bool neg = (b >> 63) != 0;
+    int E = (int)((b >> 52) & 0x7ff);
+    unsigned long long mant = b & 0xfffffffffffffull;
+    if (E) mant |= 1ull << 52; else E = 1;
+    // x * 2^(beta*S - ex[r]) as an integer, truncated: mant * 2^sh
+    const int sh = (E - 1075) + beta * S - (r < R ? ex[r] : 0);
+    unsigned long long xi = 0;
+    if (mant != 0) {
+      if (sh >= 0) xi = sh < 64 ? (mant << sh) : 0ull;
+      else xi = -sh < 64 ? (mant >> (-sh)) : 0ull;
+    }
+    const size_t plane = (size_t)Rp * Kp;
+    __nv_bfloat16* o = out + (size_t)r * Kp + k;
+    for (int s = 0; s < S; ++s) {
+      const int d = (int)((xi >> (beta * (S - 1 - s))) & dmask);
+      o[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
+    }
+  }
+}
+
+// ---- host side ------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+bool make_map(CUtensorMap* map, void* base, int S, int Rp, int Kp) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)Rp, (cuuint64_t)S};
+  const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * Rp * 2};
+  const cuuint32_t box[3] = {BKE, BM, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+constexpr size_t SMEM_BYTES = 1024 + 2 * NSTAGE * TILE_BYTES + 256;
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+SplitEngine* SplitEngine::create(int slices, int* status) {
+  *status = RGF_OK;
+  if (!encode_fn()) {
+    *status = RGF_ENOTSUP;
+    return nullptr;
+  }
+  if (cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)SMEM_BYTES) != cudaSuccess) {
+    cudaGetLastError();
+    *status = RGF_ENOTSUP;
+    return nullptr;
+  }
+  SplitEngine* e = new SplitEngine();
+  e->slices_ = slices > 0 ? slices : 6;
+  e->min_k_ = 256;
+  return e;
+}
+
+SplitEngine::~SplitEngine() {
+  if (ws_) cudaFree(ws_);
+}
+
+int SplitEngine::ensure_ws(size_t bytes) {
+  if (bytes <= ws_bytes_) return RGF_OK;
+  if (ws_) cudaFree(ws_);
+  ws_ = nullptr;
+  ws_bytes_ = 0;
+  if (cudaMalloc(&ws_, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return RGF_ENOMEM;
+  }
+  ws_bytes_ = bytes;
+  return RGF_OK;
+}
+
+int SplitEngine::reserve(int max_rows, int max_k) {
+  const size_t Rp = (size_t)round_up(std::max(max_rows, 1), BM);
+  const size_t Kp = (size_t)round_up(std::max(max_k, 1), BKE);
+  const size_t plane = (size_t)slices_ * Rp * Kp * 2;
+  return ensure_ws(2 * plane + 2 * Rp * sizeof(int) + 1024);
+}
+
+bool SplitEngine::supports(const GemmDesc& g) const {
+  return g.batch == 1 && g.k >= min_k_ && g.m > 0 && g.n > 0 &&
+         round_up(g.m, BM) <= max_rows_ && round_up(g.n, BM) <= max_rows_ &&
+         round_up(g.k, BKE) <= max_k_;
+}
+
+int SplitEngine::prepare(int max_rows, int max_k) {
+  max_rows_ = round_up(std::max(max_rows, 1), BM);
+  max_k_ = round_up(std::max(max_k, 1), BKE);
+  return reserve(max_rows_, max_k_);
+}
+
+long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st) {
+  const int S = slices_, beta = SPLIT_BETA;
+  const int Kp = round_up(g.k, BKE);
+  const int RpA = round_up(g.m, BM), RpB = round_up(g.n, BM);
+  const size_t planeA = (size_t)S * RpA * Kp, planeB = (size_t)S * RpB * Kp;
+  const size_t maxplane = (size_t)S * max_rows_ * max_k_;
+  uint8_t* base = static_cast<uint8_t*>(ws_);
+  __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(base);
+  __nv_bfloat16* sb = reinterpret_cast<__nv_bfloat16*>(base + maxplane * 2);
+  int* exA = reinterpret_cast<int*>(base + 2 * maxplane * 2);
+  int* exB = exA + max_rows_;
+  (void)planeA;
+  (void)planeB;
+  long long launched = 0;
+  // op(A) row r, term k: transA = 0 -> A[r + k*lda]; transA = 1 -> A[k + r*lda]
+  auto slice = [&](const double* X, long long rs, long long ks, int R, int tri, int* ex,
+                   __nv_bfloat16* out, int Rp) {
+    if (rs == 1)
+      row_exp_rowmajor_kernel<<<(Rp + 127) / 128, 128, 0, s>>>(X, ks, R, g.k, tri, ex, Rp);
+    else
+      row_exp_kmajor_kernel<<<(Rp * 32 + 255) / 256, 256, 0, s>>>(X, rs, R, g.k, tri, ex, Rp);
+    dim3 grid(Kp / 32, Rp / 32);
+    slice_kernel<<<grid, dim3(32, 8), 0, s>>>(X, rs, ks, R, g.k, tri, ex, out, Rp, Kp, S, beta);
+    launched += 2;
+  };
+  const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB && g.m == g.n &&
+                    g.triA == TRI_NONE && g.triB == TRI_NONE;
+  if (!g.transA) slice(g.A, 1, g.lda, g.m, g.triA, exA, sa, RpA);
+  else slice(g.A, g.lda, 1, g.m, g.triA, exA, sa, RpA);
+  // op(B)^T row c, term k: transB = 0 -> B[k + c*ldb]; transB = 1 -> B[c + k*ldb]
+  // (op(B)^T is lower when op(B) is upper and vice versa)
+  const int triBt = g.triB == TRI_LOWER ? TRI_UPPER : g.triB == TRI_UPPER ? TRI_LOWER : TRI_NONE;
+  __nv_bfloat16* sbp = sb;
+  int* exBp = exB;
+  if (same) {
+    sbp = sa;
+    exBp = exA;
+  } else if (!g.transB) {
+    slice(g.B, g.ldb, 1, g.n, triBt, exB, sb, RpB);
+  } else {
+    slice(g.B, 1, g.ldb, g.n, triBt, exB, sb, RpB);
+  }
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, sa, S, RpA, Kp) || !make_map(&mb, sbp, S, same ? RpA : RpB, Kp)) {
+    // cannot describe the operands: fall back to the FP64 kernel for this call
+    launch_gemm_fp64(g, s);
+    return launched + 1;
+  }
+  SplitParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.m = g.m; p.n = g.n; p.k = g.k;
+  p.S = S; p.beta = beta;
+  // bound of the fixed-point accumulator: K * 2^(beta*(S+1)) * 1.03 must stay below 2^62
+  const double lg = std::log2((double)g.k * 1.03) + beta * (S + 1);
+  p.cs = std::max(0, (int)std::ceil(lg) - 62);
+  int np = 0;
+  for (int lvl = 2; lvl <= S + 1; ++lvl)
+    for (int a = 1; a < lvl; ++a) {
+      const int b = lvl - a;
+      if (a <= S && b <= S && np < MAXPAIRS) {
+        p.ps[np] = (unsigned char)(a - 1);
+        p.pt[np] = (unsigned char)(b - 1);
+        ++np;
+      }
+    }
+  p.npairs = np;
+  p.triA = g.triA; p.triB = g.triB; p.outLower = g.outLower;
+  p.exA = exA; p.exB = exBp;
+  p.C = g.C; p.ldc = g.ldc; p.D = g.D; p.ldd = g.ldd;
+  p.alpha = g.alpha; p.betac = g.beta;
+  p.st = st;
+  dim3 grid(RpA / BM, RpB / BN, 1);
+  split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, p);
+  return launched + 1;
 }
 
 }  // namespace rgf

@@ -114,8 +114,15 @@ void dfree(void* p) {
 }
 
 // ---- launch wrappers (count kernels; optional event timer on bulk GEMMs) ----
-void gemm(rgf_handle* h, const GemmDesc& g, bool bulk) {
+// GEMM classes: SMALL always runs in FP64; BULK may run as split products;
+// DIAG (updates inside a diagonal block's Cholesky or inverse) runs split
+// only when the handle does not keep diagonal blocks in FP64.
+enum GemmClass { SMALL = 0, BULK = 1, DIAG = 2 };
+
+void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
+  const bool bulk = cls != SMALL;
+  const bool may_split = cls == BULK || (cls == DIAG && !h->opts.fp64_diag);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (h->timer_on && bulk) {
     if (h->ev_pool.empty()) {
@@ -129,8 +136,8 @@ void gemm(rgf_handle* h, const GemmDesc& g, bool bulk) {
     cudaEventRecord(e0, h->stream);
   }
   long long launched = 1;
-  if (h->split && bulk && g.k >= h->split->min_k())
-    launched = h->split->gemm(g, h->stream);
+  if (h->split && may_split && h->split->supports(g))
+    launched = h->split->gemm(g, h->stream, h->d_status);
   else
     launch_gemm_fp64(g, h->stream);
   h->kernels_issued += launched;
@@ -155,30 +162,42 @@ void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
 }
 
 // ---- panel Cholesky: [D; B; C] (rows x cols, lda) -> [L; B L^-T; C L^-T] ----
-// Right-looking blocked Cholesky of the top cols x cols block with the TRSM
-// of the rows below folded into each column step (RGF.H:254-260, 284-287,
-// 312-317, 335 as one pass).
+// Recursive (left half first) Cholesky of the top cols x cols block with the
+// TRSM of the rows below folded in (RGF.H:254-260, 284-287, 312-317, 335 as
+// one pass).  Halving the column range makes every trailing update one GEMM
+// with an inner dimension of half the range, so most of the work runs in a
+// few large products; 64-column leaves are factored in FP64 in one CTA and
+// solved against row-parallel.
 void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int col0,
                  int part0) {
-  int part = part0;
-  for (int k0 = 0; k0 < cols; k0 += NB) {
-    const int nbk = std::min(NB, cols - k0);
-    double* Pkk = P + k0 + (long long)k0 * lda;
-    leaf_potrf(h, Pkk, lda, nbk, col0 + k0, h->d_logpart + part++);
-    const int below = rows - (k0 + nbk);
-    if (below > 0) trsm_rows(h, Pkk + nbk, 1, lda, below, Pkk, lda, nbk, 0);
-    const int rem = cols - (k0 + nbk);
-    if (rem > 0) {
-      GemmDesc g;
-      g.m = below; g.n = rem; g.k = nbk;
-      g.A = Pkk + nbk; g.lda = lda; g.transA = 0;
-      g.B = Pkk + nbk; g.ldb = lda; g.transB = 1;
-      g.C = g.D = P + (k0 + nbk) + (long long)(k0 + nbk) * lda;
-      g.ldc = g.ldd = lda;
-      g.alpha = -1.0; g.beta = 1.0; g.outLower = 1;
-      gemm(h, g, true);
-    }
+  if (cols <= NB) {
+    leaf_potrf(h, P, lda, cols, col0, h->d_logpart + part0);
+    if (rows > cols) trsm_rows(h, P + cols, 1, lda, rows - cols, P, lda, cols, 0);
+    return;
   }
+  const int c1 = ((cols / 2 + NB - 1) / NB) * NB;
+  panel_potrf(h, P, lda, rows, c1, col0, part0);
+  // trailing update: P[c1:rows, c1:cols] -= P[c1:rows, 0:c1] P[c1:cols, 0:c1]^T
+  auto upd = [&](int r0, int m, int cls) {
+    GemmDesc g;
+    g.m = m; g.n = cols - c1; g.k = c1;
+    g.A = P + r0; g.lda = lda; g.transA = 0;
+    g.B = P + c1; g.ldb = lda; g.transB = 1;
+    g.C = g.D = P + r0 + (long long)c1 * lda;
+    g.ldc = g.ldd = lda;
+    g.alpha = -1.0; g.beta = 1.0;
+    // lower-only when the block starts on the diagonal (rows below it are full)
+    g.outLower = r0 < cols ? 1 : 0;
+    gemm(h, g, cls);
+  };
+  if (h->split && h->opts.fp64_diag) {
+    upd(c1, cols - c1, DIAG);              // inside the diagonal block: FP64
+    if (rows > cols) upd(cols, rows - cols, BULK);
+  } else {
+    upd(c1, rows - c1, BULK);
+  }
+  panel_potrf(h, P + c1 + (long long)c1 * lda, lda, rows - c1, cols - c1, col0 + c1,
+              part0 + c1 / NB);
 }
 
 // ---- stage 1: factorize (RGF.H:233-340) ----
@@ -203,7 +222,7 @@ void issue_factor(rgf_handle* h) {
       g.A = Pm + ns; g.lda = ldm; g.B = Pm + ns; g.ldb = ldm; g.transB = 1;
       g.C = g.D = P; g.ldc = g.ldd = lda;
       g.alpha = -1.0; g.beta = 1.0; g.outLower = 1;
-      gemm(h, g, true);
+      gemm(h, g, BULK);
       if (nd > 0) {
         const double* Cm = Pm + mf_dense_row(sh, i - 1);
         GemmDesc a;  // C_i -= C_{i-1} L_{i,i-1}^T  (RGF.H:279, 307)
@@ -211,13 +230,13 @@ void issue_factor(rgf_handle* h) {
         a.A = Cm; a.lda = ldm; a.B = Pm + ns; a.ldb = ldm; a.transB = 1;
         a.C = a.D = P + mf_dense_row(sh, i); a.ldc = a.ldd = lda;
         a.alpha = -1.0; a.beta = 1.0;
-        gemm(h, a, true);
+        gemm(h, a, BULK);
         GemmDesc c;  // corner -= C_{i-1} C_{i-1}^T  (RGF.H:280, 308)
         c.m = c.n = (int)nd; c.k = (int)ns;
         c.A = Cm; c.lda = ldm; c.B = Cm; c.ldb = ldm; c.transB = 1;
         c.C = c.D = corner; c.ldc = c.ldd = nd;
         c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
-        gemm(h, c, false);
+        gemm(h, c, SMALL);
       }
     }
     panel_potrf(h, P, lda, (int)lda, (int)ns, (int)(i * ns), (int)(i * tiles));
@@ -230,7 +249,7 @@ void issue_factor(rgf_handle* h) {
     c.A = Cl; c.lda = mf_lda(sh, nt - 1); c.B = Cl; c.ldb = mf_lda(sh, nt - 1); c.transB = 1;
     c.C = c.D = corner; c.ldc = c.ldd = nd;
     c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
-    gemm(h, c, false);
+    gemm(h, c, SMALL);
     panel_potrf(h, corner, nd, (int)nd, (int)nd, (int)(nt * ns), (int)(nt * tiles));  // RGF.H:335
   }
   launch_logdet_reduce(h->d_logpart, h->nparts, h->d_scalars, s);
@@ -260,7 +279,7 @@ void issue_trtri(rgf_handle* h, double* U, long long ldu, long long m, const dou
       g.C = g.D = U + (k0 + nbk) * ldu; g.ldc = g.ldd = ldu;
       g.alpha = -1.0; g.beta = 1.0;
       g.batch = batch; g.sA = sU; g.sB = sL; g.sC = g.sD = sU;
-      gemm(h, g, true);
+      gemm(h, g, DIAG);
     }
   }
 }
@@ -294,7 +313,7 @@ void issue_selinv(rgf_handle* h) {
   if (nd > 0) {
     issue_trtri(h, Ud, nd, nd, h->d_MF + mf_col_offset(sh, nt), nd, 1, 0, 0);
     // Sigma_dd = L_dd^{-T} L_dd^{-1} = U_d U_d^T   (RGF.H:439-442)
-    gemm(h, mk(ind, ind, ind, Ud, nd, 0, Ud, nd, 1, nullptr, 0, Sdd, nd, 1.0, 0.0), false);
+    gemm(h, mk(ind, ind, ind, Ud, nd, 0, Ud, nd, 1, nullptr, 0, Sdd, nd, 1.0, 0.0), SMALL);
   }
   const bool compat = h->opts.selinv_mode == RGF_SELINV_COMPAT;
   for (long long i = nt - 1; i >= 0; --i) {
@@ -311,61 +330,61 @@ void issue_selinv(rgf_handle* h) {
     if (!compat) {
       if (has_next) {
         // X = Sigma_{i+1,i+1} L_{i+1,i} + Sigma_{d,i+1}^T C_i
-        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), true);
+        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), BULK);
         if (nd > 0)
           gemm(h, mk(ins, ins, ind, Sdn, ldn, 1, Ci, lda, 0, h->d_T1, ns, h->d_T1, ns, 1.0, 1.0),
-               false);
+               SMALL);
         // Sigma_{i+1,i} = -X L_ii^{-1} = -X U_i^T
         GemmDesc g = mk(ins, ins, ins, h->d_T1, ns, 0, Ui, ns, 1, nullptr, 0, Q + ns, lda, -1.0, 0.0);
         g.triB = TRI_LOWER;
-        gemm(h, g, true);
+        gemm(h, g, BULK);
       }
       if (nd > 0) {
         // Y = Sigma_dd C_i + Sigma_{d,i+1} L_{i+1,i};  Sigma_{d,i} = -Y U_i^T
-        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), false);
+        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), SMALL);
         if (has_next)
           gemm(h, mk(ind, ins, ins, Sdn, ldn, 0, Bi, lda, 0, h->d_T3, nd, h->d_T3, nd, 1.0, 1.0),
-               true);
+               BULK);
         GemmDesc g = mk(ind, ins, ins, h->d_T3, nd, 0, Ui, ns, 1, nullptr, 0,
                         Q + mf_dense_row(sh, i), lda, -1.0, 0.0);
         g.triB = TRI_LOWER;
-        gemm(h, g, true);
+        gemm(h, g, BULK);
       }
       // W^T = U_i - Sigma_{i+1,i}^T L_{i+1,i} - Sigma_{d,i}^T C_i
       if (has_next) {
-        gemm(h, mk(ins, ins, ins, Q + ns, lda, 1, Bi, lda, 0, Ui, ns, h->d_T2, ns, -1.0, 1.0), true);
+        gemm(h, mk(ins, ins, ins, Q + ns, lda, 1, Bi, lda, 0, Ui, ns, h->d_T2, ns, -1.0, 1.0), BULK);
       } else {
         launch_copy(Ui, ns, h->d_T2, ns, ins, ins, 1, 0, 0, s);
         h->kernels_issued++;
       }
       if (nd > 0)
         gemm(h, mk(ins, ins, ind, Q + mf_dense_row(sh, i), lda, 1, Ci, lda, 0, h->d_T2, ns,
-                   h->d_T2, ns, -1.0, 1.0), false);
+                   h->d_T2, ns, -1.0, 1.0), SMALL);
       // Sigma_ii = L_ii^{-T} W = U_i (W^T)^T
       GemmDesc g = mk(ins, ins, ins, Ui, ns, 0, h->d_T2, ns, 1, nullptr, 0, Q, lda, 1.0, 0.0);
       g.triA = TRI_UPPER;
-      gemm(h, g, true);
+      gemm(h, g, BULK);
     } else {
       // the reference's recursion (RGF.H:444-502):
       // Sigma_ii = L^{-T} (I + B^T Sigma_{i+1,i+1} B + C^T Sigma_dd C) L^{-1}
       launch_set_identity(h->d_T2, ns, ins, 1, 0, s);
       h->kernels_issued++;
       if (has_next) {
-        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), true);
+        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), BULK);
         gemm(h, mk(ins, ins, ins, Bi, lda, 1, h->d_T1, ns, 0, h->d_T2, ns, h->d_T2, ns, 1.0, 1.0),
-             true);
+             BULK);
       }
       if (nd > 0) {
-        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), false);
+        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), SMALL);
         gemm(h, mk(ins, ins, ind, Ci, lda, 1, h->d_T3, nd, 0, h->d_T2, ns, h->d_T2, ns, 1.0, 1.0),
-             false);
+             SMALL);
       }
       GemmDesc g1 = mk(ins, ins, ins, h->d_T2, ns, 0, Ui, ns, 1, nullptr, 0, h->d_T1, ns, 1.0, 0.0);
       g1.triB = TRI_LOWER;
-      gemm(h, g1, true);
+      gemm(h, g1, BULK);
       GemmDesc g2 = mk(ins, ins, ins, Ui, ns, 0, h->d_T1, ns, 0, nullptr, 0, Q, lda, 1.0, 0.0);
       g2.triA = TRI_UPPER;
-      gemm(h, g2, true);
+      gemm(h, g2, BULK);
     }
   }
   launch_extract_diag(sh, h->d_MS, h->d_diag, s);
@@ -382,7 +401,7 @@ void trsv_lower(rgf_handle* h, const double* L, long long ldl, int m, double* R,
     const int rem = m - k0 - nbk;
     if (rem > 0)
       gemm(h, mk(rem, nrhs, nbk, Lkk + nbk, ldl, 0, R + k0, ldr, 0, R + k0 + nbk, ldr,
-                 R + k0 + nbk, ldr, -1.0, 1.0), false);
+                 R + k0 + nbk, ldr, -1.0, 1.0), SMALL);
   }
 }
 
@@ -396,7 +415,7 @@ void trsv_lower_t(rgf_handle* h, const double* L, long long ldl, int m, double* 
     const double* Lkk = L + k0 + (long long)k0 * ldl;
     trsm_rows(h, R + k0, ldr, 1, nrhs, Lkk, ldl, nbk, 1);
     if (k0 > 0)
-      gemm(h, mk(k0, nrhs, nbk, L + k0, ldl, 1, R + k0, ldr, 0, R, ldr, R, ldr, -1.0, 1.0), false);
+      gemm(h, mk(k0, nrhs, nbk, L + k0, ldl, 1, R + k0, ldr, 0, R, ldr, R, ldr, -1.0, 1.0), SMALL);
   }
 }
 
@@ -413,7 +432,7 @@ void issue_solve(rgf_handle* h, int nrhs) {
     if (i > 0) {
       const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
       gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 0, R + (i - 1) * ns, n, 0,
-                 R + i * ns, n, R + i * ns, n, -1.0, 1.0), false);       // RGF.H:365
+                 R + i * ns, n, R + i * ns, n, -1.0, 1.0), SMALL);       // RGF.H:365
     }
     trsv_lower(h, P, lda, ins, R + i * ns, n, nrhs);                      // RGF.H:356,367
   }
@@ -428,11 +447,11 @@ void issue_solve(rgf_handle* h, int nrhs) {
       GemmDesc g = mk(ins, nrhs, ind, h->d_MF + 2 * ns, 2 * ns + nd, 1, R + nt * ns, n, 0, R, n, R,
                       n, -1.0, 1.0);
       g.batch = (int)(nt - 1); g.sA = ns * (2 * ns + nd); g.sB = 0; g.sC = g.sD = ns;
-      gemm(h, g, false);
+      gemm(h, g, SMALL);
     }
     const double* Pl = h->d_MF + mf_col_offset(sh, nt - 1);
     gemm(h, mk(ins, nrhs, ind, Pl + ns, ns + nd, 1, R + nt * ns, n, 0, R + (nt - 1) * ns, n,
-               R + (nt - 1) * ns, n, -1.0, 1.0), false);
+               R + (nt - 1) * ns, n, -1.0, 1.0), SMALL);
   }
   for (long long i = nt - 1; i >= 0; --i) {
     const double* P = h->d_MF + mf_col_offset(sh, i);
@@ -440,7 +459,7 @@ void issue_solve(rgf_handle* h, int nrhs) {
     if (i > 0) {
       const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
       gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 1, R + i * ns, n, 0,
-                 R + (i - 1) * ns, n, R + (i - 1) * ns, n, -1.0, 1.0), false);  // RGF.H:410
+                 R + (i - 1) * ns, n, R + (i - 1) * ns, n, -1.0, 1.0), SMALL);  // RGF.H:410
     }
   }
 }
@@ -652,6 +671,9 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     if (o.precision == RGF_PREC_SPLIT) {
       h->split = SplitEngine::create(o.slices, &st);
       if (st) break;
+      // operands have at most 2ns+nd rows and ns (or nd) terms
+      st = h->split->prepare((int)(2 * ns + nd), (int)std::max(ns, nd));
+      if (st) break;
     }
     // validate the pattern once on the device
     status_init_kernel<<<1, 1, 0, h->stream>>>(h->d_status);
@@ -830,6 +852,49 @@ int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launc
     h->timer_launches = 0;
   }
   return RGF_OK;
+}
+
+int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m, int n, int k,
+                     double alpha, const double* A, int lda, const double* B, int ldb,
+                     double beta, double* C, int ldc, void* stream) {
+  if (m < 0 || n < 0 || k < 0 || !C || (k > 0 && (!A || !B))) return RGF_EINVAL;
+  if (precision != RGF_PREC_FP64 && precision != RGF_PREC_SPLIT) return RGF_EINVAL;
+  if (slices < 0 || slices > 8) return RGF_EINVAL;
+  const bool ta = transa == 'T' || transa == 't', tb = transb == 'T' || transb == 't';
+  if (lda < std::max(1, ta ? k : m) || ldb < std::max(1, tb ? n : k) || ldc < std::max(1, m))
+    return RGF_EINVAL;
+  if (m == 0 || n == 0) return RGF_OK;
+  GemmDesc g;
+  g.m = m; g.n = n; g.k = k;
+  g.A = A; g.lda = lda; g.transA = ta;
+  g.B = B; g.ldb = ldb; g.transB = tb;
+  g.C = C; g.ldc = ldc; g.D = C; g.ldd = ldc;
+  g.alpha = alpha; g.beta = beta;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DevStatus* st = nullptr;
+  RGF_CK(cudaMalloc(&st, sizeof(DevStatus)));
+  RGF_CK(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
+  int status = RGF_OK;
+  SplitEngine* eng = nullptr;
+  if (precision == RGF_PREC_SPLIT) {
+    eng = SplitEngine::create(slices, &status);
+    if (!status) status = eng->prepare(std::max(m, n), k);
+  }
+  if (!status) {
+    if (eng && eng->supports(g)) eng->gemm(g, s, st);
+    else launch_gemm_fp64(g, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) status = cuda_status(e);
+  }
+  if (!status) {
+    DevStatus hs;
+    if (cudaMemcpy(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost) != cudaSuccess) status = RGF_ECUDA;
+    else if (hs.timeout) status = RGF_ETIMEOUT;
+  }
+  delete eng;
+  cudaFree(st);
+  return status;
 }
 
 int rgf_measure_fp64_peak(double* tflops) {

@@ -1,8 +1,10 @@
 // Split-precision (Ozaki-scheme) GEMM engine: FP64 operands are cut into
-// bf16 slices, slice products run on the tcgen05 tensor cores with FP32
+// bf16 digit slices, slice products run on the tcgen05 tensor cores with FP32
 // accumulation in tensor memory, and the exact partial sums are combined in
 // 64-bit integer fixed point before one conversion back to FP64.
 #pragma once
+
+#include <cstddef>
 
 #include "rgf_internal.h"
 
@@ -10,18 +12,29 @@ namespace rgf {
 
 class SplitEngine {
  public:
-  // Returns nullptr and sets *status on failure.
+  // Returns nullptr and sets *status when the device or driver cannot run it.
   static SplitEngine* create(int slices, int* status);
   ~SplitEngine();
-  // Smallest inner dimension routed to the split path.
+  // Size the slice workspace for operands of up to max_rows rows and max_k
+  // terms (allocates once, outside any graph capture).
+  int prepare(int max_rows, int max_k);
+  // True when g can run on the tensor cores (single problem, k >= min_k and
+  // within the prepared sizes).
+  bool supports(const GemmDesc& g) const;
+  int slices() const { return slices_; }
   int min_k() const { return min_k_; }
-  // Issue D = alpha op(A) op(B) + beta C; returns the kernels launched.
-  long long gemm(const GemmDesc& g, cudaStream_t s);
+  // Issue D = alpha op(A) op(B) + beta C on stream s; returns kernels launched.
+  long long gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st);
 
  private:
   SplitEngine() = default;
+  int ensure_ws(size_t bytes);
+  int reserve(int max_rows, int max_k);
   int slices_ = 0;
   int min_k_ = 1 << 30;
+  int max_rows_ = 0, max_k_ = 0;
+  void* ws_ = nullptr;
+  size_t ws_bytes_ = 0;
 };
 
 }  // namespace rgf
