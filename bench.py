@@ -41,6 +41,7 @@ WORKLOADS = {
     "ns3_nt3_nd2": dict(ns=3, nt=3, nd=2, seed=1, spde=None),
     # a 20-block prefix of the default workload, for profiling runs
     "ns2000_nt20_nd6": dict(ns=2000, nt=20, nd=6, seed=3, spde=None),
+    "ns2000_nt5_nd6": dict(ns=2000, nt=5, nd=6, seed=3, spde=None),
 }
 METRIC = "FP64-equiv TFLOP/s for factorize+logDet+RGFdiag"
 
@@ -107,6 +108,19 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    """bf16 peaks from MEASURED_PEAKS.json (measured on this GPU pool), else the
+    documented fallback."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return {"bf16": float(p["bf16_tflops"]),
+                "bf16_sustained": float(p["bf16_tflops_sustained"])}, "of measured"
+    except Exception:
+        return {"bf16": 1900.0, "bf16_sustained": 1700.0}, "of fallback"
 
 
 def make_inputs(w):
@@ -200,7 +214,7 @@ def run_rgf(args, w):
     del ia, ja, a
 
     s = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
-                      slices=args.slices, device=dev)
+                      slices=args.slices, device=dev, fp64_diag=not args.no_fp64_diag)
     stream = torch.cuda.ExternalStream(s.stream())
 
     def step():
@@ -212,7 +226,7 @@ def run_rgf(args, w):
         step()
     torch.cuda.synchronize()
     k0 = s.info()["kernels_launched"]
-    s.kernel_timer(True)
+    s.kernel_timer(2 if os.environ.get("RGF_GB300_TIMER_DETAIL") else 1)
     s.kernel_timer_read(reset=True)
     clocks = Clocks(dev)
     if dist:
@@ -246,7 +260,7 @@ def run_rgf(args, w):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
-                          slices=args.slices, device=dev)
+                          slices=args.slices, device=dev, fp64_diag=not args.no_fp64_diag)
         h.factorize()
         h.logDet()
         h.RGFdiag(diag_host)
@@ -262,18 +276,37 @@ def run_rgf(args, w):
     h2d = ia_p.nbytes + ja_p.nbytes + a_p.nbytes
     d2h = diag_host.nbytes + 8
 
-    # roofline of the dominant kernel: FP64 DMMA GEMM vs measured FP64 peak
-    peak = rgf_gb300.measure_fp64_peak()
-    per_launch_flops = timer["flops"] / max(1, timer["launches"])
-    per_launch_ms = timer["ms"] / max(1, timer["launches"])
-    achieved = per_launch_flops / (per_launch_ms * 1e-3) / 1e12 if timer["launches"] else None
-    roofline = {"bound": "tensor", "kernel": "gemm_fp64_kernel (DMMA m8n8k4)",
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if achieved else None, "traffic": None,
-                "peak_source": "FP64 DMMA m8n8k4 loop measured in this run (the peaks file "
-                               "has no FP64 figure)",
-                "kernel_share_of_step": timer["ms"] / ms_total if ms_total else None,
-                "launches_per_step": timer["launches"] / args.steps}
+    # roofline of the dominant kernel class (timed live over the timed region)
+    peak64 = rgf_gb300.measure_fp64_peak()
+    peaks, src = load_peaks()
+    fp, sp = timer["fp64"], timer["split"]
+    kernels = {
+        "gemm_fp64_kernel": {"ms_per_step": fp["ms"] / args.steps,
+                             "launches_per_step": fp["launches"] / args.steps,
+                             "fp64_equiv_tflops": fp["flops"] / max(fp["ms"], 1e-9) / 1e9},
+        "split_gemm (slice + tcgen05)": {
+            "ms_per_step": sp["ms"] / args.steps, "launches_per_step": sp["launches"] / args.steps,
+            "fp64_equiv_tflops": sp["flops"] / max(sp["ms"], 1e-9) / 1e9,
+            "tensor_tflops": sp["tensor_flops"] / max(sp["ms"], 1e-9) / 1e9},
+    }
+    if sp["ms"] > fp["ms"]:
+        ach = sp["tensor_flops"] / (sp["ms"] * 1e-3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "split_gemm_kernel (tcgen05 bf16 slices)",
+                    "achieved": ach, "peak": peaks["bf16_sustained"], "unit": "TFLOP/s",
+                    "frac": ach / peaks["bf16_sustained"], "traffic": None,
+                    "peak_source": f"bf16 sustained, {src}",
+                    "achieved_counts": "executed bf16 slice-product flops (pairs x 2MNK) / "
+                                       "kernel time incl. slicing",
+                    "kernel_share_of_step": sp["ms"] / ms_total}
+    else:
+        ach = fp["flops"] / (fp["ms"] * 1e-3) / 1e12 if fp["ms"] else None
+        roofline = {"bound": "tensor", "kernel": "gemm_fp64_kernel (DMMA m8n8k4)",
+                    "achieved": ach, "peak": peak64, "unit": "TFLOP/s",
+                    "frac": ach / peak64 if ach else None, "traffic": None,
+                    "peak_source": "FP64 DMMA m8n8k4 loop measured in this run (the peaks file "
+                                   "has no FP64 figure)",
+                    "kernel_share_of_step": fp["ms"] / ms_total}
+    roofline["kernels"] = kernels
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -287,6 +320,7 @@ def run_rgf(args, w):
                 "dtype": "f64" if args.precision == "fp64" else "bf16-slices/f64",
                 "data": "synthetic",
                 "config": {"workload": args.workload, **cfg_of(w), "precision": args.precision,
+                           "fp64_diag": not args.no_fp64_diag, "slices": args.slices or 6,
                            "l2": "inputs larger than L2 (CSC %.1f GB, factor %.1f GB)" % (
                                h2d / 1e9, s.info()["mf_size"] * 8 / 1e9)},
                 "e2e": ({"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
@@ -311,6 +345,8 @@ def main():
     p.add_argument("--workload", choices=sorted(WORKLOADS), default="ns2000_nt100_nd6")
     p.add_argument("--precision", choices=["fp64", "split"], default="fp64")
     p.add_argument("--slices", type=int, default=0)
+    p.add_argument("--no-fp64-diag", action="store_true",
+                   help="split precision: also run the diagonal blocks' inner updates as split products")
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--ref-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")

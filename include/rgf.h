@@ -47,13 +47,15 @@ enum rgf_selinv_mode {
 
 typedef struct rgf_opts {
   int precision;    /* enum rgf_precision (default RGF_PREC_FP64)             */
-  int slices;       /* split precision: slices per operand, 0 = default       */
+  int slices;       /* split precision: 7-bit slices per operand (1..8),
+                       0 = default 6 (42-bit operands)                        */
   int selinv_mode;  /* enum rgf_selinv_mode (default RGF_SELINV_EXACT)        */
   int device;       /* CUDA device ordinal, -1 = the current device           */
   int use_graphs;   /* 1 = replay each stage as a captured CUDA graph         */
-  int fp64_diag;    /* split precision: 1 (default) keeps the Cholesky and the
-                       inverse of every diagonal block entirely in FP64; 0 runs
-                       their large inner updates as split products too        */
+  int fp64_diag;    /* split precision, Cholesky and inverse of the diagonal
+                       blocks: 1 (default) FP64 accuracy, their inner products
+                       emulated with 8 slices (56-bit operands); 2 native FP64
+                       units; 0 the bulk slice count                          */
   int reserved[10];
 } rgf_opts;
 
@@ -136,12 +138,15 @@ int rgf_diag_device(rgf_handle* h, const double** d_diag);
 int rgf_get_stream(rgf_handle* h, void** stream);
 
 /* Kernel timer: while enabled, every launch of the bulk GEMM kernels of this
- * handle is bracketed by CUDA events on the handle's stream; *ms receives the
- * summed device time, *launches their number and *flops their algorithmic
- * FP64-equivalent flops since the last reset.  Stages run without CUDA graphs
- * while the timer is enabled. */
+ * handle is bracketed by CUDA events on the handle's stream.  For kind
+ * 0 (all bulk GEMMs), 1 (FP64 DMMA GEMM) or 2 (split tensor-core GEMM, including
+ * its slicing kernels) *ms receives the summed device time, *launches their
+ * number and *flops their algorithmic FP64-equivalent flops since the last
+ * reset; kind 3 reports the split GEMMs with *flops = executed bf16
+ * slice-product flops.  Stages run without CUDA graphs while it is enabled.
+ * enable = 2 also prints per-shape totals to stderr at each reset. */
 int rgf_kernel_timer_enable(rgf_handle* h, int enable);
-int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launches,
+int rgf_kernel_timer_read(rgf_handle* h, int reset, int kind, double* ms, long long* launches,
                           double* flops);
 
 /* C := alpha op(A) op(B) + beta C on device memory (column-major, BLAS

@@ -75,7 +75,7 @@ _SIGS = {
     "rgf_dgemm_device": (C.c_int, [C.c_int, C.c_int, C.c_char, C.c_char, C.c_int, C.c_int,
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p,
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
-    "rgf_kernel_timer_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+    "rgf_kernel_timer_read": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double),
                                         C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
 }
 
@@ -137,7 +137,7 @@ class RGF:
 
     def __init__(self, ia, ja, a, ns: int, nt: int, nd: int, precision: str = "fp64",
                  slices: int = 0, selinv: str = "exact", device: int = -1,
-                 use_graphs: bool = True, fp64_diag: bool = True):
+                 use_graphs: bool = True, fp64_diag=1):
         lib = load_library()
         self._lib = lib
         self._h = C.c_void_p()
@@ -158,7 +158,9 @@ class RGF:
         o.selinv_mode = SELINV[selinv]
         o.device = int(device)
         o.use_graphs = 1 if use_graphs else 0
-        o.fp64_diag = 1 if fp64_diag else 0
+        # True/1: FP64-accurate emulated diagonal blocks, "native"/2: FP64
+        # units, False/0: bulk slice count
+        o.fp64_diag = {True: 1, False: 0, "native": 2}.get(fp64_diag, fp64_diag)
         _check(lib.rgf_create(_ptr(self._ia), _ptr(self._ja), _ptr(self._a), self.ns, self.nt,
                               self.nd, C.byref(o), C.byref(self._h)), "rgf_create")
 
@@ -248,14 +250,23 @@ class RGF:
         _check(self._lib.rgf_get_stream(self._h, C.byref(p)), "rgf_get_stream")
         return p.value or 0
 
-    def kernel_timer(self, enable: bool) -> None:
-        _check(self._lib.rgf_kernel_timer_enable(self._h, 1 if enable else 0), "timer")
+    def kernel_timer(self, enable) -> None:
+        """True/1: time bulk GEMMs; 2: also print per-shape totals on reset."""
+        _check(self._lib.rgf_kernel_timer_enable(self._h, int(enable)), "timer")
 
     def kernel_timer_read(self, reset: bool = True) -> dict:
-        ms, n, fl = C.c_double(), C.c_longlong(), C.c_double()
-        _check(self._lib.rgf_kernel_timer_read(self._h, 1 if reset else 0, C.byref(ms),
-                                               C.byref(n), C.byref(fl)), "timer")
-        return {"ms": ms.value, "launches": n.value, "flops": fl.value}
+        """Per class: 'all', 'fp64' (DMMA GEMM), 'split' (tensor-core GEMM) with
+        ms, launches and FP64-equivalent flops; 'split' also has tensor_flops."""
+        out = {}
+        for kind, name in ((0, "all"), (1, "fp64"), (2, "split"), (3, "split_tensor")):
+            ms, n, fl = C.c_double(), C.c_longlong(), C.c_double()
+            _check(self._lib.rgf_kernel_timer_read(self._h, 0, kind, C.byref(ms), C.byref(n),
+                                                   C.byref(fl)), "timer")
+            out[name] = {"ms": ms.value, "launches": n.value, "flops": fl.value}
+        out["split"]["tensor_flops"] = out.pop("split_tensor")["flops"]
+        if reset:
+            _check(self._lib.rgf_kernel_timer_read(self._h, 1, 0, None, None, None), "timer")
+        return out
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:

@@ -5,6 +5,7 @@
 // pipe, not by memory: 64x64 output tiles, 4 warps of 32x32 built from
 // m8n8k4 DMMA fragments, operands staged through shared memory with a
 // register prefetch of the next K slice.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -40,7 +41,8 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
   const int m0 = blockIdx.x * GBM;
   const int n0 = blockIdx.y * GBN;
   if (g.outLower && m0 + GBM <= n0) return;  // tile entirely above the diagonal
-  const long long bz = blockIdx.z;
+  const bool splitk = g.ksplit > 1;              // blockIdx.z is the K slice, batch == 1
+  const long long bz = splitk ? 0 : blockIdx.z;
   const double* __restrict__ A = g.A + bz * g.sA;
   const double* __restrict__ B = g.B + bz * g.sB;
   const double* C = g.C ? g.C + bz * g.sC : nullptr;
@@ -52,7 +54,14 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
-  const GemmTileRange kr = k_range(g, m0, n0);
+  GemmTileRange kr = k_range(g, m0, n0);
+  if (splitk) {
+    const int len = max(0, kr.khi - kr.klo);
+    const int chunk = ((len + g.ksplit - 1) / g.ksplit + GBK - 1) / GBK * GBK;
+    const int lo = kr.klo + (int)blockIdx.z * chunk;
+    kr.khi = min(kr.khi, lo + chunk);
+    kr.klo = lo;
+  }
 
   double acc[4][4][2];
 #pragma unroll
@@ -121,6 +130,21 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
     }
   }
 
+  if (splitk) {  // raw partial sums of this K slice; reduced in fixed order later
+    double* W = g.ws + (long long)blockIdx.z * g.m * g.n;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = m0 + wm + i * 8 + (lane >> 2);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int c = n0 + wn + j * 8 + (lane & 3) * 2 + e;
+          if (r < g.m && c < g.n) W[(long long)r + (long long)c * g.m] = acc[i][j][e];
+        }
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int r = m0 + wm + i * 8 + (lane >> 2);
@@ -141,69 +165,93 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
 }
 
 // ---------------------------------------------------------------------------
-// Leaf Cholesky of one <= 64 x 64 diagonal tile, right-looking in shared memory.
-// GB300's FP64 pipe retires about two lanes per cycle per SM, so every FP64
-// warp instruction is expensive: the pivot's reciprocal square root is formed
-// once per column by one warp (an FP32 seed refined by two Newton steps), the
-// trailing update maps warps to columns and lanes to rows (no index
-// arithmetic per element), and the tile's 64 logs run in parallel.
+// Leaf Cholesky of one <= 64 x 64 diagonal tile in shared memory.
+// On GB300 each SM sub-partition has its own FP64 unit; one FP64 warp
+// instruction occupies it ~80 cycles and a dependent FP64 op waits ~64, so the
+// column-to-column pivot chain (next pivot update, its reciprocal square root)
+// is the critical path.  Warp 0 runs that chain alone on sub-partition 0;
+// warps on the other three sub-partitions apply the rank-1 updates from the
+// unscaled column with a per-column factor S[c][j] * y_j^2; all scaling to L
+// happens in one parallel pass at the end; the tile's log-sum uses parallel
+// logs and a fixed-order reduction.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double rsqrt_newton(double d) {
-  // d > 0 and normal: d = m * 4^k with m in [1, 4)
+// reciprocal square root of a normal positive double: exponent split with
+// integer ops, an FP32 seed from the top mantissa bits (no FP64 conversion
+// instructions) and two Newton steps in FP64
+__device__ __forceinline__ double rsqrt_fast(double d) {
   const long long b = __double_as_longlong(d);
   const int e = (int)((b >> 52) & 0x7ff) - 1023;
-  if (e == -1023) return 1.0 / sqrt(d);  // subnormal pivot
-  const int k = e >> 1;
-  const double m = __longlong_as_double(b - ((long long)(2 * k) << 52));
-  double y = (double)rsqrtf((float)m);
+  if (e == -1023) return 1.0 / sqrt(d);                   // subnormal pivot
+  const int k = e >> 1;                                   // d = m * 4^k, m in [1, 4)
+  const long long mb = b - ((long long)(2 * k) << 52);
+  const double m = __longlong_as_double(mb);
+  // float with the same value as m up to 23 mantissa bits
+  const unsigned int fb = (unsigned int)(((mb >> 52) - 1023 + 127) << 23) |
+                          (unsigned int)((mb >> 29) & 0x7fffff);
+  const float yf = rsqrtf(__uint_as_float(fb));
+  const unsigned int yb = __float_as_uint(yf);
+  double y = __longlong_as_double((long long)(((yb >> 23) & 0xff) - 127 + 1023) << 52 |
+                                  ((long long)(yb & 0x7fffff) << 29));
   const double hm = 0.5 * m;
   y = y * fma(-hm, y * y, 1.5);
   y = y * fma(-hm, y * y, 1.5);
   return y * __longlong_as_double((long long)(1023 - k) << 52);
 }
 
+
 __global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ldt, int nbk,
                                                          int col0, double* logpart,
                                                          DevStatus* st) {
+  // warp 0 (sub-partition 0) runs the pivot chain alone; warps 1,2,3,5,6,7
+  // (sub-partitions 1..3) apply the trailing updates; warp 4 shares
+  // sub-partition 0 with warp 0 and stays out of the loop.  S keeps the
+  // unscaled columns; all scaling happens once at the end.
   __shared__ double S[64][65];
-  __shared__ double piv[2];
-  __shared__ double lg[64];
+  __shared__ double ys[64];
   __shared__ int fail;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
-  for (int c = warp; c < nbk; c += nw)
-    for (int r = lane; r < nbk; r += 32)
-      S[r][c] = (r >= c) ? T[(long long)r + (long long)c * ldt] : 0.0;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  for (int c = warp; c < nbk; c += 8)
+    for (int r = c + lane; r < nbk; r += 32) S[r][c] = T[(long long)r + (long long)c * ldt];
   if (tid == 0) fail = -1;
   __syncthreads();
+  // trailing-warp index 0..5 for warps 1,2,3,5,6,7
+  const int tw = warp < 4 ? warp - 1 : warp - 2;
+  if (tid == 0) {
+    const double d = S[0][0];
+    if (!(d > 0.0)) fail = 0;
+    ys[0] = d > 0.0 ? rsqrt_fast(d) : nan;
+  }
+  __syncthreads();
   for (int j = 0; j < nbk; ++j) {
+    const double y = ys[j];
     if (warp == 0) {
-      const double d = S[j][j];
-      const bool ok = d > 0.0;
-      const double y = rsqrt_newton(ok ? d : 1.0);
-      if (lane == 0) {
-        if (!ok && fail < 0) fail = j;
-        const double nan = __longlong_as_double(0x7ff8000000000000LL);
-        piv[0] = ok ? d * y : nan;  // L_jj
-        piv[1] = ok ? y : nan;      // 1 / L_jj
+      if (lane == 0 && j + 1 < nbk) {
+        const double s = S[j + 1][j] * y;
+        const double d = fma(-s, s, S[j + 1][j + 1]);
+        const bool ok = d > 0.0;
+        if (!ok && fail < 0) fail = j + 1;
+        ys[j + 1] = ok ? rsqrt_fast(d) : nan;
+        S[j + 1][j + 1] = d;
+      }
+    } else if (warp != 4) {
+      const double y2 = y * y;
+      for (int c = j + 1 + tw; c < nbk; c += 6) {
+        const double f = S[c][j] * y2;
+        const int r0 = c + lane + (c == j + 1 ? 1 : 0);
+        for (int r = r0; r < nbk; r += 32) S[r][c] = fma(-S[r][j], f, S[r][c]);
       }
     }
     __syncthreads();
-    const double rinv = piv[1];
-    for (int r = j + 1 + tid; r < nbk; r += blockDim.x) S[r][j] *= rinv;
-    if (tid == 0) S[j][j] = piv[0];
-    __syncthreads();
-    for (int c = j + 1 + warp; c < nbk; c += nw) {
-      const double ljc = S[c][j];
-      for (int r = c + lane; r < nbk; r += 32) S[r][c] = fma(-S[r][j], ljc, S[r][c]);
-    }
-    __syncthreads();
   }
-  for (int c = warp; c < nbk; c += nw)
-    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c];
-  if (tid < nbk) lg[tid] = log(S[tid][tid]);
-  __syncthreads();
+  // L = S scaled column-wise: L_rj = S_rj * y_j (r > j), L_jj = S_jj * y_j
+  for (int c = warp; c < nbk; c += 8) {
+    const double y = ys[c];
+    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c] * y;
+  }
   if (warp == 0) {
-    double v = (lane < nbk ? lg[lane] : 0.0) + (lane + 32 < nbk ? lg[lane + 32] : 0.0);
+    double v = (lane < nbk ? log(S[lane][lane] * ys[lane]) : 0.0) +
+               (lane + 32 < nbk ? log(S[lane + 32][lane + 32] * ys[lane + 32]) : 0.0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) {
@@ -214,55 +262,105 @@ __global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ld
 }
 
 // ---------------------------------------------------------------------------
-// Row-parallel triangular solve with a <= 64 x 64 lower tile: each thread
-// owns one row of X in registers; the tile is broadcast from shared memory.
+// Row-parallel triangular solve with a <= 64 x 64 lower tile.  On GB300 each
+// SM sub-partition has its own slow FP64 unit (a dependent DFMA takes ~64
+// cycles; one warp reaches a quarter of the SM's FP64 rate), so a CTA is
+// four warps sharing 32 rows: lane t owns row t (column t of Xs) and warp w
+// applies the updates of the unknowns l = w, w+4, ... after each x_j is
+// final.  Loops stay rolled (a fully unrolled solve stalls on instruction
+// fetch).
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(32) trsm_rows_kernel(double* X, long long xrs, long long xcs,
-                                                        int rows, const double* L, long long ldl,
-                                                        int nbk, long long sX, long long sL) {
+__global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs, long long xcs,
+                                                         int rows, const double* L, long long ldl,
+                                                         int nbk, long long sX, long long sL) {
   __shared__ double Ls[64][65];
+  __shared__ double Xs[64][33];
   __shared__ double rinv[64];
   X += (long long)blockIdx.y * sX;
   L += (long long)blockIdx.y * sL;
-  for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+  const int t = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 128) {
     const int c = idx >> 6, r = idx & 63;
     double v = 0.0;
     if (r < nbk && c < nbk && r >= c) v = L[(long long)r + (long long)c * ldl];
     Ls[r][c] = v;
   }
+  const long long r = (long long)blockIdx.x * 32 + t;
+  const bool live = r < rows;
+  for (int j = w; j < nbk; j += 4) Xs[j][t] = live ? X[r * xrs + (long long)j * xcs] : 0.0;
   __syncthreads();
-  for (int j = threadIdx.x; j < 64; j += blockDim.x) rinv[j] = (j < nbk) ? 1.0 / Ls[j][j] : 0.0;
+  if (threadIdx.x < 64) rinv[threadIdx.x] = (threadIdx.x < nbk) ? 1.0 / Ls[threadIdx.x][threadIdx.x] : 0.0;
   __syncthreads();
-  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  double x[64];
-#pragma unroll
-  for (int j = 0; j < 64; ++j) x[j] = (j < nbk) ? X[r * xrs + (long long)j * xcs] : 0.0;
-  if (MODE == 0) {
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-      if (j < nbk) {
-        double s = x[j];
-#pragma unroll
-        for (int l = 0; l < j; ++l) s = fma(-x[l], Ls[j][l], s);
-        x[j] = s * rinv[j];
-      }
+  if (MODE == 0) {  // x_j = (b_j - sum_{l<j} x_l L_jl) / L_jj
+    for (int j = 0; j < nbk; ++j) {
+      const double xj = Xs[j][t] * rinv[j];
+      __syncthreads();  // every warp has read x_j before it is overwritten
+      if (w == 0) Xs[j][t] = xj;
+      // first unknown > j owned by this warp
+      const int l0 = j + 1 + ((w - (j + 1)) % 4 + 4) % 4;
+#pragma unroll 4
+      for (int l = l0; l < nbk; l += 4) Xs[l][t] = fma(-xj, Ls[l][j], Xs[l][t]);
+      __syncthreads();
     }
-  } else {
+  } else {  // x_j = (b_j - sum_{l>j} x_l L_lj) / L_jj, j descending
+    for (int j = nbk - 1; j >= 0; --j) {
+      const double xj = Xs[j][t] * rinv[j];
+      __syncthreads();
+      if (w == 0) Xs[j][t] = xj;
+#pragma unroll 4
+      for (int l = w; l < j; l += 4) Xs[l][t] = fma(-xj, Ls[j][l], Xs[l][t]);
+      __syncthreads();
+    }
+  }
+  if (live)
+    for (int j = w; j < nbk; j += 4) X[r * xrs + (long long)j * xcs] = Xs[j][t];
+}
+
+// Thin products (m <= 16, op(B) = B^T): lane = output column, the 4 warps of
+// a CTA split a K chunk, blockIdx.y selects the chunk.  Partial sums go to
+// the split-K workspace in the GEMM kernel's layout.
+__global__ void __launch_bounds__(128) gemm_thin_m_kernel(GemmDesc g, int kchunk) {
+  __shared__ double red[4][16][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + lane;
+  const int k0 = blockIdx.y * kchunk, k1 = min(g.k, k0 + kchunk);
+  double acc[16];
 #pragma unroll
-    for (int j = 63; j >= 0; --j) {
-      if (j < nbk) {
-        double s = x[j];
+  for (int r = 0; r < 16; ++r) acc[r] = 0.0;
+  if (c < g.n) {
+    for (int k = k0 + w; k < k1; k += 4) {
+      if (g.triB == TRI_LOWER && k < c) continue;   // op(B)(k, c) = 0 above
+      if (g.triB == TRI_UPPER && k > c) continue;
+      const double b = g.B[(long long)c + (long long)k * g.ldb];
+      const double* a = g.transA ? g.A + (long long)k : g.A + (long long)k * g.lda;
 #pragma unroll
-        for (int l = j + 1; l < 64; ++l) s = fma(-x[l], Ls[l][j], s);  // x[l] = 0 beyond nbk
-        x[j] = s * rinv[j];
-      }
+      for (int r = 0; r < 16; ++r)
+        if (r < g.m) acc[r] = fma(g.transA ? a[(long long)r * g.lda] : a[r], b, acc[r]);
     }
   }
 #pragma unroll
-  for (int j = 0; j < 64; ++j)
-    if (j < nbk) X[r * xrs + (long long)j * xcs] = x[j];
+  for (int r = 0; r < 16; ++r) red[w][r][lane] = acc[r];
+  __syncthreads();
+  if (w == 0 && c < g.n) {
+    double* W = g.ws + (long long)blockIdx.y * g.m * g.n;
+#pragma unroll
+    for (int r = 0; r < 16; ++r)
+      if (r < g.m) W[(long long)r + (long long)c * g.m] =
+          ((red[0][r][lane] + red[1][r][lane]) + red[2][r][lane]) + red[3][r][lane];
+  }
+}
+
+// D = alpha * sum_s W_s + beta * C over the split-K partials, in slice order.
+__global__ void splitk_reduce_kernel(GemmDesc g) {
+  const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
+  if (r >= g.m || c >= g.n || (g.outLower && r < c)) return;
+  const long long mn = (long long)g.m * g.n, o = (long long)r + (long long)c * g.m;
+  double v = 0.0;
+  for (int s = 0; s < g.ksplit; ++s) v += g.ws[s * mn + o];
+  v *= g.alpha;
+  if (g.beta != 0.0) v += g.beta * g.C[(long long)r + (long long)c * g.ldc];
+  g.D[(long long)r + (long long)c * g.ldd] = v;
 }
 
 }  // namespace
@@ -276,10 +374,46 @@ double gemm_flops(const GemmDesc& g) {
   return f * g.batch;
 }
 
-void launch_gemm_fp64(const GemmDesc& g, cudaStream_t s) {
-  if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
-  dim3 grid((g.m + GBM - 1) / GBM, (g.n + GBN - 1) / GBN, g.batch);
+int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
+  if (g0.m <= 0 || g0.n <= 0 || g0.batch <= 0) return 0;
+  GemmDesc g = g0;
+  if (g.m <= 16 && g.transB && g.triA == TRI_NONE && g.batch == 1 && g.ws && !g.outLower) {
+    const int cx = (g.n + 31) / 32;
+    int kchunks = std::max(1, std::min((2 * 152 + cx - 1) / cx, (g.k + 63) / 64));
+    while (kchunks > 1 && (long long)kchunks * g.m * g.n > g.ws_elems) --kchunks;
+    if ((long long)kchunks * g.m * g.n <= g.ws_elems) {
+      const int kchunk = (g.k + kchunks - 1) / kchunks;
+      g.ksplit = kchunks;
+      gemm_thin_m_kernel<<<dim3(cx, kchunks), 128, 0, s>>>(g, kchunk);
+      dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
+      splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
+      return 2;
+    }
+  }
+  const int tx = (g.m + GBM - 1) / GBM, ty = (g.n + GBN - 1) / GBN;
+  // too few output tiles for 152 SMs (each SM retires only ~3.5 FP64 flops
+  // per cycle, so one 64x64x64 tile is tens of microseconds): split K
+  int ksplit = 1;
+  if (g.batch == 1 && g.ws && g.k >= 32) {
+    long long tiles = 0;
+    for (int bx = 0; bx < tx; ++bx)
+      for (int by = 0; by < ty; ++by)
+        if (!(g.outLower && bx * GBM + GBM <= by * GBN)) ++tiles;
+    if (tiles > 0 && tiles < 2 * 152) {
+      ksplit = (int)std::min<long long>(16, (3 * 152 + tiles - 1) / tiles);
+      ksplit = std::min(ksplit, g.k / 16);
+      while (ksplit > 1 && (long long)ksplit * g.m * g.n > g.ws_elems) --ksplit;
+    }
+  }
+  g.ksplit = ksplit;
+  dim3 grid(tx, ty, ksplit > 1 ? ksplit : g.batch);
   gemm_fp64_kernel<<<grid, 128, 0, s>>>(g);
+  if (ksplit > 1) {
+    dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
+    splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
+    return 2;
+  }
+  return 1;
 }
 
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, double* logpart,
@@ -294,9 +428,9 @@ void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const d
   if (rows <= 0 || nbk <= 0 || batch <= 0) return;
   dim3 grid((rows + 31) / 32, batch);
   if (mode == 0)
-    trsm_rows_kernel<0><<<grid, 32, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+    trsm_rows_kernel<0><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
   else
-    trsm_rows_kernel<1><<<grid, 32, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+    trsm_rows_kernel<1><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
 }
 
 }  // namespace rgf

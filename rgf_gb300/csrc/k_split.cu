@@ -52,10 +52,11 @@ struct SplitParams {
   int triA, triB, outLower;
   const int* exA;
   const int* exB;
+  int exA_stride, exB_stride;   // per batch item (padded rows)
   const double* C;
-  long long ldc;
+  long long ldc, sC;
   double* D;
-  long long ldd;
+  long long ldd, sD;
   double alpha, betac;
   DevStatus* st;
 };
@@ -207,6 +208,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   if (p.outLower && m0 + BM <= n0) return;  // whole tile above the diagonal (uniform exit)
+  const int zb = blockIdx.z;                // batch item: slice planes zb*S .. zb*S+S-1
+  const int zS = zb * p.S;
 
   int kb_lo, kb_hi;
   tile_kblocks(p, m0, n0, kb_lo, kb_hi);
@@ -249,8 +252,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
           if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, p.st)) break;
           mbar_expect_tx(&full[s], 2 * TILE_BYTES);
-          tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], kb * BKE, m0, p.ps[pr]);
-          tma_load_3d(tilesB + s * TILE_BYTES, &tmB, &full[s], kb * BKE, n0, p.pt[pr]);
+          tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], kb * BKE, m0, zS + p.ps[pr]);
+          tma_load_3d(tilesB + s * TILE_BYTES, &tmB, &full[s], kb * BKE, n0, zS + p.pt[pr]);
         }
       }
       // let in-flight loads land before the CTA can exit
@@ -328,15 +331,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // epilogue: one FP64 conversion per output
     const int r = m0 + row;
     if (r < p.m && !*abort_flag) {
-      const int er = p.exA[r] + p.cs - p.beta * (p.S + 1);
+      const int* exB = p.exB + (long long)zb * p.exB_stride;
+      const double* C = p.C ? p.C + (long long)zb * p.sC : nullptr;
+      double* D = p.D + (long long)zb * p.sD;
+      const int er = p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1);
       const int cbase = n0 + half * 64;
 #pragma unroll
       for (int i = 0; i < 64; ++i) {
         const int c = cbase + i;
         if (c < p.n && !(p.outLower && r < c)) {
-          double v = p.alpha * ((double)acc[i] * pow2(er + p.exB[c]));
-          if (p.betac != 0.0) v += p.betac * p.C[(long long)r + (long long)c * p.ldc];
-          p.D[(long long)r + (long long)c * p.ldd] = v;
+          double v = p.alpha * ((double)acc[i] * pow2(er + exB[c]));
+          if (p.betac != 0.0) v += p.betac * C[(long long)r + (long long)c * p.ldc];
+          D[(long long)r + (long long)c * p.ldd] = v;
         }
       }
     }
@@ -363,50 +369,64 @@ __device__ __forceinline__ int exp_of_max(unsigned long long mx) {
   return (E == 0 ? -1022 : E - 1023) + 1;
 }
 
-// one thread per row, rows contiguous (rs == 1): coalesced across the warp
-__global__ void row_exp_rowmajor_kernel(const double* X, long long ks, int R, int K, int tri,
-                                        int* ex, int Rp) {
+// rows contiguous (rs == 1): thread per row, blockIdx.y picks a 32-term
+// slice of K, partial maxima of |x| (as bit patterns) meet in atomicMax.
+__global__ void rowmax_rowmajor_kernel(const double* X, long long ks, int R, int K, int tri,
+                                       unsigned long long* mx, long long sX, int Rp) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= Rp) return;
-  unsigned long long mx = 0;
-  if (r < R)
-    for (int k = 0; k < K; ++k)
-      if (tri_ok(tri, r, k)) {
-        const unsigned long long b =
-            (unsigned long long)__double_as_longlong(X[r + (long long)k * ks]) &
-            0x7fffffffffffffffull;
-        mx = b > mx ? b : mx;
-      }
-  ex[r] = exp_of_max(mx);
+  if (r >= R) return;
+  X += (long long)blockIdx.z * sX;
+  mx += (long long)blockIdx.z * Rp;
+  const int k0 = blockIdx.y * 32, k1 = min(K, k0 + 32);
+  unsigned long long m = 0;
+#pragma unroll 8
+  for (int k = k0; k < k1; ++k) {  // independent loads in flight
+    const unsigned long long b =
+        (unsigned long long)__double_as_longlong(X[r + (long long)k * ks]) & 0x7fffffffffffffffull;
+    if (tri_ok(tri, r, k)) m = b > m ? b : m;
+  }
+  if (m) atomicMax(&mx[r], m);
 }
 
-// one warp per row, k contiguous (ks == 1)
-__global__ void row_exp_kmajor_kernel(const double* X, long long rs, int R, int K, int tri,
-                                      int* ex, int Rp) {
+// k contiguous (ks == 1): one warp per row
+__global__ void rowmax_kmajor_kernel(const double* X, long long rs, int R, int K, int tri,
+                                     unsigned long long* mx, int Rp, long long sX) {
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (r >= Rp) return;
-  unsigned long long mx = 0;
+  X += (long long)blockIdx.y * sX;
+  mx += (long long)blockIdx.y * Rp;
+  unsigned long long m = 0;
   if (r < R)
     for (int k = lane; k < K; k += 32)
       if (tri_ok(tri, r, k)) {
         const unsigned long long b =
             (unsigned long long)__double_as_longlong(X[(long long)r * rs + k]) &
             0x7fffffffffffffffull;
-        mx = b > mx ? b : mx;
+        m = b > m ? b : m;
       }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = y > mx ? y : mx;
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
   }
-  if (lane == 0) ex[r] = exp_of_max(mx);
+  if (lane == 0) mx[r] = m;
+}
+
+__global__ void row_exp_kernel(const unsigned long long* mx, int* ex, int Rp) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long o = (long long)blockIdx.y * Rp;
+  if (r < Rp) ex[o + r] = exp_of_max(mx[o + r]);
 }
 
 // 32 x 32 tiles through shared memory: read coalesced along the contiguous
 // dimension, write the S digit planes coalesced along k.
 __global__ void slice_kernel(const double* X, long long rs, long long ks, int R, int K, int tri,
-                             const int* ex, __nv_bfloat16* out, int Rp, int Kp, int S, int beta) {
+                             const int* ex, __nv_bfloat16* out, int Rp, int Kp, int S, int beta,
+                             long long sX) {
   __shared__ double tile[32][33];
+  X += (long long)blockIdx.z * sX;
+  ex += (long long)blockIdx.z * Rp;
+  out += (size_t)blockIdx.z * S * Rp * Kp;
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
 #pragma unroll
@@ -498,7 +518,7 @@ SplitEngine* SplitEngine::create(int slices, int* status) {
   }
   SplitEngine* e = new SplitEngine();
   e->slices_ = slices > 0 ? slices : 6;
-  e->min_k_ = 256;
+  e->min_k_ = 64;
   return e;
 }
 
@@ -519,15 +539,26 @@ int SplitEngine::ensure_ws(size_t bytes) {
   return RGF_OK;
 }
 
+namespace {
+constexpr int MAX_SLICES = 8;
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+// bytes of workspace one batch item of an (RpA x Kp) by (RpB x Kp) problem needs
+size_t item_bytes(int S, int RpA, int RpB, int Kp) {
+  return align256((size_t)S * RpA * Kp * 2) + align256((size_t)S * RpB * Kp * 2) +
+         align256((size_t)(RpA + RpB) * sizeof(int)) +
+         align256((size_t)(RpA + RpB) * sizeof(unsigned long long));
+}
+}  // namespace
+
 int SplitEngine::reserve(int max_rows, int max_k) {
-  const size_t Rp = (size_t)round_up(std::max(max_rows, 1), BM);
-  const size_t Kp = (size_t)round_up(std::max(max_k, 1), BKE);
-  const size_t plane = (size_t)slices_ * Rp * Kp * 2;
-  return ensure_ws(2 * plane + 2 * Rp * sizeof(int) + 1024);
+  // one problem of the largest size at the largest slice count, and at least
+  // 1 GiB so that batched problems run in few chunks
+  const size_t one = item_bytes(MAX_SLICES, max_rows, max_rows, max_k);
+  return ensure_ws(std::max(one, (size_t)1 << 30) + 1024);
 }
 
 bool SplitEngine::supports(const GemmDesc& g) const {
-  return g.batch == 1 && g.k >= min_k_ && g.m > 0 && g.n > 0 &&
+  return g.k >= min_k_ && g.m > 0 && g.n > 0 && g.batch >= 1 &&
          round_up(g.m, BM) <= max_rows_ && round_up(g.n, BM) <= max_rows_ &&
          round_up(g.k, BKE) <= max_k_;
 }
@@ -538,54 +569,17 @@ int SplitEngine::prepare(int max_rows, int max_k) {
   return reserve(max_rows_, max_k_);
 }
 
-long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st) {
-  const int S = slices_, beta = SPLIT_BETA;
+long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
+                            double* tensor_flops, int slices) {
+  if (tensor_flops) *tensor_flops = 0.0;
+  const int S = slices > 0 ? std::min(slices, MAX_SLICES) : slices_, beta = SPLIT_BETA;
   const int Kp = round_up(g.k, BKE);
   const int RpA = round_up(g.m, BM), RpB = round_up(g.n, BM);
-  const size_t planeA = (size_t)S * RpA * Kp, planeB = (size_t)S * RpB * Kp;
-  const size_t maxplane = (size_t)S * max_rows_ * max_k_;
-  uint8_t* base = static_cast<uint8_t*>(ws_);
-  __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(base);
-  __nv_bfloat16* sb = reinterpret_cast<__nv_bfloat16*>(base + maxplane * 2);
-  int* exA = reinterpret_cast<int*>(base + 2 * maxplane * 2);
-  int* exB = exA + max_rows_;
-  (void)planeA;
-  (void)planeB;
-  long long launched = 0;
-  // op(A) row r, term k: transA = 0 -> A[r + k*lda]; transA = 1 -> A[k + r*lda]
-  auto slice = [&](const double* X, long long rs, long long ks, int R, int tri, int* ex,
-                   __nv_bfloat16* out, int Rp) {
-    if (rs == 1)
-      row_exp_rowmajor_kernel<<<(Rp + 127) / 128, 128, 0, s>>>(X, ks, R, g.k, tri, ex, Rp);
-    else
-      row_exp_kmajor_kernel<<<(Rp * 32 + 255) / 256, 256, 0, s>>>(X, rs, R, g.k, tri, ex, Rp);
-    dim3 grid(Kp / 32, Rp / 32);
-    slice_kernel<<<grid, dim3(32, 8), 0, s>>>(X, rs, ks, R, g.k, tri, ex, out, Rp, Kp, S, beta);
-    launched += 2;
-  };
-  const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB && g.m == g.n &&
-                    g.triA == TRI_NONE && g.triB == TRI_NONE;
-  if (!g.transA) slice(g.A, 1, g.lda, g.m, g.triA, exA, sa, RpA);
-  else slice(g.A, g.lda, 1, g.m, g.triA, exA, sa, RpA);
-  // op(B)^T row c, term k: transB = 0 -> B[k + c*ldb]; transB = 1 -> B[c + k*ldb]
-  // (op(B)^T is lower when op(B) is upper and vice versa)
-  const int triBt = g.triB == TRI_LOWER ? TRI_UPPER : g.triB == TRI_UPPER ? TRI_LOWER : TRI_NONE;
-  __nv_bfloat16* sbp = sb;
-  int* exBp = exB;
-  if (same) {
-    sbp = sa;
-    exBp = exA;
-  } else if (!g.transB) {
-    slice(g.B, g.ldb, 1, g.n, triBt, exB, sb, RpB);
-  } else {
-    slice(g.B, 1, g.ldb, g.n, triBt, exB, sb, RpB);
-  }
-  CUtensorMap ma, mb;
-  if (!make_map(&ma, sa, S, RpA, Kp) || !make_map(&mb, sbp, S, same ? RpA : RpB, Kp)) {
-    // cannot describe the operands: fall back to the FP64 kernel for this call
-    launch_gemm_fp64(g, s);
-    return launched + 1;
-  }
+  const bool same = g.A == g.B && g.lda == g.ldb && g.sA == g.sB && g.transA != g.transB &&
+                    g.m == g.n && g.triA == TRI_NONE && g.triB == TRI_NONE;
+  const size_t per_item = item_bytes(S, RpA, same ? 0 : RpB, Kp);
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(g.batch, ws_bytes_ / per_item));
+  // the split itself: pairs (s, t) with s + t <= S + 1, ordered by level
   SplitParams p;
   std::memset(&p, 0, sizeof(p));
   p.m = g.m; p.n = g.n; p.k = g.k;
@@ -605,13 +599,76 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st) {
     }
   p.npairs = np;
   p.triA = g.triA; p.triB = g.triB; p.outLower = g.outLower;
-  p.exA = exA; p.exB = exBp;
-  p.C = g.C; p.ldc = g.ldc; p.D = g.D; p.ldd = g.ldd;
+  p.ldc = g.ldc; p.ldd = g.ldd; p.sC = g.sC; p.sD = g.sD;
   p.alpha = g.alpha; p.betac = g.beta;
   p.st = st;
-  dim3 grid(RpA / BM, RpB / BN, 1);
-  split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, p);
-  return launched + 1;
+  p.exA_stride = RpA; p.exB_stride = same ? RpA : RpB;
+  const int triBt = g.triB == TRI_LOWER ? TRI_UPPER : g.triB == TRI_UPPER ? TRI_LOWER : TRI_NONE;
+  long long launched = 0;
+  uint8_t* base = static_cast<uint8_t*>(ws_);
+  for (int b0 = 0; b0 < g.batch; b0 += chunk) {
+    const int nbat = std::min(chunk, g.batch - b0);
+    uint8_t* q = base;
+    __nv_bfloat16* sa = reinterpret_cast<__nv_bfloat16*>(q); q += align256((size_t)nbat * S * RpA * Kp * 2);
+    __nv_bfloat16* sb = same ? sa : reinterpret_cast<__nv_bfloat16*>(q);
+    if (!same) q += align256((size_t)nbat * S * RpB * Kp * 2);
+    int* exA = reinterpret_cast<int*>(q); q += align256((size_t)nbat * RpA * sizeof(int));
+    int* exB = same ? exA : reinterpret_cast<int*>(q);
+    if (!same) q += align256((size_t)nbat * RpB * sizeof(int));
+    unsigned long long* mxA = reinterpret_cast<unsigned long long*>(q);
+    q += align256((size_t)nbat * RpA * sizeof(unsigned long long));
+    unsigned long long* mxB = reinterpret_cast<unsigned long long*>(q);
+    // rows of op(X): (r, k) at X[r*rs + k*ks]; digits into out, exponents into ex
+    auto slice = [&](const double* X, long long rs, long long ks, long long sX, int R, int tri,
+                     int* ex, unsigned long long* mx, __nv_bfloat16* out, int Rp) {
+      if (rs == 1) {
+        cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rp * nbat, s);
+        dim3 grid((R + 127) / 128, (g.k + 31) / 32, nbat);
+        rowmax_rowmajor_kernel<<<grid, 128, 0, s>>>(X, ks, R, g.k, tri, mx, sX, Rp);
+      } else {
+        dim3 grid((Rp * 32 + 255) / 256, nbat);
+        rowmax_kmajor_kernel<<<grid, 256, 0, s>>>(X, rs, R, g.k, tri, mx, Rp, sX);
+      }
+      row_exp_kernel<<<dim3((Rp + 255) / 256, nbat), 256, 0, s>>>(mx, ex, Rp);
+      dim3 grid(Kp / 32, Rp / 32, nbat);
+      slice_kernel<<<grid, dim3(32, 8), 0, s>>>(X, rs, ks, R, g.k, tri, ex, out, Rp, Kp, S, beta,
+                                                sX);
+      launched += 3;
+    };
+    const double* A = g.A + (long long)b0 * g.sA;
+    if (!g.transA) slice(A, 1, g.lda, g.sA, g.m, g.triA, exA, mxA, sa, RpA);
+    else slice(A, g.lda, 1, g.sA, g.m, g.triA, exA, mxA, sa, RpA);
+    if (!same) {
+      const double* B = g.B + (long long)b0 * g.sB;
+      if (!g.transB) slice(B, g.ldb, 1, g.sB, g.n, triBt, exB, mxB, sb, RpB);
+      else slice(B, 1, g.ldb, g.sB, g.n, triBt, exB, mxB, sb, RpB);
+    }
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, sa, S * nbat, RpA, Kp) ||
+        !make_map(&mb, sb, S * nbat, same ? RpA : RpB, Kp)) {
+      GemmDesc f = g;  // cannot describe the operands: FP64 kernel for this chunk
+      f.batch = nbat;
+      f.A = A; f.B = g.B + (long long)b0 * g.sB;
+      f.C = g.C ? g.C + (long long)b0 * g.sC : nullptr;
+      f.D = g.D + (long long)b0 * g.sD;
+      launched += launch_gemm_fp64(f, s);
+      continue;
+    }
+    p.exA = exA; p.exB = exB;
+    p.C = g.C ? g.C + (long long)b0 * g.sC : nullptr;
+    p.D = g.D + (long long)b0 * g.sD;
+    dim3 grid(RpA / BM, RpB / BN, nbat);
+    if (tensor_flops) {
+      double tiles = 0.0;  // lower-only outputs skip tiles above the diagonal
+      for (int bx = 0; bx < (int)grid.x; ++bx)
+        for (int by = 0; by < (int)grid.y; ++by)
+          if (!(g.outLower && bx * BM + BM <= by * BN)) tiles += 1.0;
+      *tensor_flops += tiles * nbat * 2.0 * BM * BN * (double)Kp * np;
+    }
+    split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, p);
+    launched += 1;
+  }
+  return launched;
 }
 
 }  // namespace rgf

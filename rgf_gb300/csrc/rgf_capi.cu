@@ -12,9 +12,11 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "../../include/rgf.h"
@@ -53,6 +55,8 @@ struct rgf_handle {
   double* d_partial = nullptr;  // arrowhead partial sums, nt * nrhs * nd
   size_t partial_cap = 0;
   double* d_res = nullptr;      // residual scratch: x, b, y (3n)
+  double* d_gemm_ws = nullptr;  // split-K partial sums of small FP64 GEMMs
+  long long gemm_ws_elems = 0;
 
   bool factored = false;
   bool selinv_done = false;
@@ -66,12 +70,23 @@ struct rgf_handle {
   long long kernels_total = 0;    // kernels launched over the handle's life
 
   SplitEngine* split = nullptr;
+  int nb = 64;  // leaf width of the panel Cholesky (<= 64)
 
+  // kernel timer: per class (1 = FP64 DMMA GEMM, 2 = split tensor-core GEMM)
+  struct TimedLaunch {
+    cudaEvent_t e0, e1;
+    int kind;
+    double flops;         // algorithmic FP64-equivalent flops
+    double tensor_flops;  // executed bf16 slice-product flops (split only)
+    int m, n, k, batch, cls;
+  };
+  std::map<std::string, std::pair<long long, double>> timer_detail;  // shape -> (launches, ms)
   bool timer_on = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_used, ev_pool;
-  std::vector<double> ev_flops;
-  double timer_ms = 0.0, timer_flops = 0.0;
-  long long timer_launches = 0;
+  bool timer_detail_on = false;  // per-shape totals printed to stderr on timer reset
+  std::vector<TimedLaunch> ev_used;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+  double timer_ms[3] = {0, 0, 0}, timer_flops[3] = {0, 0, 0}, timer_tflops = 0.0;
+  long long timer_launches[3] = {0, 0, 0};
 };
 
 namespace {
@@ -122,7 +137,11 @@ enum GemmClass { SMALL = 0, BULK = 1, DIAG = 2 };
 void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
   const bool bulk = cls != SMALL;
-  const bool may_split = cls == BULK || (cls == DIAG && !h->opts.fp64_diag);
+  // fp64_diag: 0 = diagonal blocks at the bulk slice count, 1 = at 8 slices
+  // (56-bit operands: FP64-accurate emulation), 2 = native FP64 DMMA
+  const int fd = h->opts.fp64_diag;
+  const bool may_split = cls == BULK || (cls == DIAG && fd != 2);
+  const int slices = (cls == DIAG && fd == 1) ? 8 : 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (h->timer_on && bulk) {
     if (h->ev_pool.empty()) {
@@ -136,15 +155,35 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
     cudaEventRecord(e0, h->stream);
   }
   long long launched = 1;
-  if (h->split && may_split && h->split->supports(g))
-    launched = h->split->gemm(g, h->stream, h->d_status);
-  else
-    launch_gemm_fp64(g, h->stream);
+  double tflops = 0.0;
+  bool split = h->split && may_split && h->split->supports(g);
+  if (split) {
+    // Route by estimated time.  A split product has a fixed cost of a few
+    // small slicing kernels and tensor tiles padded to 128 x 128; the FP64
+    // DMMA kernel (split-K for small grids) has almost none but runs at
+    // ~1 TFLOP/s.  Small or thin products are faster in FP64 (which is also
+    // FP64-accurate).
+    const int S = slices > 0 ? slices : h->split->slices();
+    const double pairs = S * (S + 1) / 2.0;
+    auto up = [](double x, double m) { return std::ceil(x / m) * m; };
+    const double t_split = (g.A == g.B ? 40e-6 : 70e-6) +
+                           pairs * 2.0 * up(g.m, 128) * up(g.n, 128) * up(g.k, 64) * g.batch /
+                               700e12;
+    const double t_fp64 = 8e-6 + gemm_flops(g) / 0.8e12;
+    split = t_split < t_fp64;
+  }
+  if (split) {
+    launched = h->split->gemm(g, h->stream, h->d_status, &tflops, slices);
+  } else {
+    GemmDesc gw = g;
+    gw.ws = h->d_gemm_ws;
+    gw.ws_elems = h->gemm_ws_elems;
+    launched = launch_gemm_fp64(gw, h->stream);
+  }
   h->kernels_issued += launched;
   if (e0) {
     cudaEventRecord(e1, h->stream);
-    h->ev_used.push_back({e0, e1});
-    h->ev_flops.push_back(gemm_flops(g));
+    h->ev_used.push_back({e0, e1, split ? 2 : 1, gemm_flops(g), tflops, g.m, g.n, g.k, g.batch, cls});
   }
 }
 
@@ -170,12 +209,13 @@ void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
 // solved against row-parallel.
 void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int col0,
                  int part0) {
-  if (cols <= NB) {
+  const int nb = h->nb;
+  if (cols <= nb) {
     leaf_potrf(h, P, lda, cols, col0, h->d_logpart + part0);
     if (rows > cols) trsm_rows(h, P + cols, 1, lda, rows - cols, P, lda, cols, 0);
     return;
   }
-  const int c1 = ((cols / 2 + NB - 1) / NB) * NB;
+  const int c1 = ((cols / 2 + nb - 1) / nb) * nb;
   panel_potrf(h, P, lda, rows, c1, col0, part0);
   // trailing update: P[c1:rows, c1:cols] -= P[c1:rows, 0:c1] P[c1:cols, 0:c1]^T
   auto upd = [&](int r0, int m, int cls) {
@@ -191,13 +231,13 @@ void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, in
     gemm(h, g, cls);
   };
   if (h->split && h->opts.fp64_diag) {
-    upd(c1, cols - c1, DIAG);              // inside the diagonal block: FP64
+    upd(c1, cols - c1, DIAG);              // inside the diagonal block: FP64 accuracy
     if (rows > cols) upd(cols, rows - cols, BULK);
   } else {
     upd(c1, rows - c1, BULK);
   }
   panel_potrf(h, P + c1 + (long long)c1 * lda, lda, rows - c1, cols - c1, col0 + c1,
-              part0 + c1 / NB);
+              part0 + c1 / nb);
 }
 
 // ---- stage 1: factorize (RGF.H:233-340) ----
@@ -210,7 +250,7 @@ void issue_factor(rgf_handle* h) {
   launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, s);
   h->kernels_issued += 2;
   double* corner = h->d_MF + mf_col_offset(sh, nt);
-  const int tiles = (int)((ns + NB - 1) / NB);
+  const int tiles = (int)((ns + h->nb - 1) / h->nb);
   for (long long i = 0; i < nt; ++i) {
     double* P = h->d_MF + mf_col_offset(sh, i);
     const long long lda = mf_lda(sh, i);
@@ -261,27 +301,43 @@ void issue_factor(rgf_handle* h) {
 // current block are non-zero, so the work is ns^3/3 per block.  The
 // nt-1 blocks of leading dimension 2ns+nd run as one batch, the last block
 // (leading dimension ns+nd) and the corner separately.
-void issue_trtri(rgf_handle* h, double* U, long long ldu, long long m, const double* L,
-                 long long ldl, int batch, long long sU, long long sL) {
-  if (batch <= 0 || m <= 0) return;
-  launch_set_identity(U, ldu, (int)m, batch, sU, h->stream);
-  h->kernels_issued++;
-  for (long long k0 = 0; k0 < m; k0 += NB) {
-    const int nbk = (int)std::min<long long>(NB, m - k0);
-    trsm_rows(h, U + k0 * ldu, 1, ldu, (int)(k0 + nbk), L + k0 + k0 * ldl, ldl, nbk, 0, batch,
-              sU, sL);
-    const long long rem = m - k0 - nbk;
-    if (rem > 0) {
-      GemmDesc g;
-      g.m = (int)(k0 + nbk); g.n = (int)rem; g.k = nbk;
-      g.A = U + k0 * ldu; g.lda = ldu;
-      g.B = L + (k0 + nbk) + k0 * ldl; g.ldb = ldl; g.transB = 1;
-      g.C = g.D = U + (k0 + nbk) * ldu; g.ldc = g.ldd = ldu;
-      g.alpha = -1.0; g.beta = 1.0;
-      g.batch = batch; g.sA = sU; g.sB = sL; g.sC = g.sD = sU;
-      gemm(h, g, DIAG);
-    }
+// For `batch` diagonal blocks at once: U = L^{-T} (upper triangular).
+// Recursive halving: with L = [L11 0; L21 L22], U = [U11 U12; 0 U22] where
+// U11 = L11^{-T}, U22 = L22^{-T} and U12 = -U11 (L21^T U22).  The two halves
+// are independent; each level adds two GEMMs with an inner dimension of half
+// the range, batched over all blocks, so the inverse runs as a few large
+// products (DIAG class: FP64 or FP64-accurate split).  Leaves (<= 64) solve
+// X L^T = I row-parallel.  T (the product L21^T U22) lives in Tmp at the
+// position of U12.
+void issue_trtri(rgf_handle* h, double* U, long long ldu, long long n, const double* L,
+                 long long ldl, double* Tmp, long long ldt, int batch, long long sU, long long sL,
+                 long long sT) {
+  if (batch <= 0 || n <= 0) return;
+  if (n <= NB) {
+    launch_set_identity(U, ldu, (int)n, batch, sU, h->stream);
+    h->kernels_issued++;
+    trsm_rows(h, U, 1, ldu, (int)n, L, ldl, (int)n, 0, batch, sU, sL);
+    return;
   }
+  const long long n1 = ((n / 2 + NB - 1) / NB) * NB, n2 = n - n1;
+  issue_trtri(h, U, ldu, n1, L, ldl, Tmp, ldt, batch, sU, sL, sT);
+  issue_trtri(h, U + n1 + n1 * ldu, ldu, n2, L + n1 + n1 * ldl, ldl, Tmp + n1 + n1 * ldt, ldt,
+              batch, sU, sL, sT);
+  double* T = Tmp + n1 * ldt;
+  GemmDesc a;  // T = L21^T U22
+  a.m = (int)n1; a.n = (int)n2; a.k = (int)n2;
+  a.A = L + n1; a.lda = ldl; a.transA = 1;
+  a.B = U + n1 + n1 * ldu; a.ldb = ldu; a.triB = TRI_UPPER;
+  a.D = T; a.ldd = ldt; a.alpha = 1.0; a.beta = 0.0;
+  a.batch = batch; a.sA = sL; a.sB = sU; a.sD = sT;
+  gemm(h, a, DIAG);
+  GemmDesc b;  // U12 = -U11 T
+  b.m = (int)n1; b.n = (int)n2; b.k = (int)n1;
+  b.A = U; b.lda = ldu; b.triA = TRI_UPPER;
+  b.B = T; b.ldb = ldt;
+  b.D = U + n1 * ldu; b.ldd = ldu; b.alpha = -1.0; b.beta = 0.0;
+  b.batch = batch; b.sA = sU; b.sB = sT; b.sD = sU;
+  gemm(h, b, DIAG);
 }
 
 GemmDesc mk(int m, int n, int k, const double* A, long long lda, int tA, const double* B,
@@ -307,11 +363,12 @@ void issue_selinv(rgf_handle* h) {
   double* Sdd = h->d_MS + mf_col_offset(sh, nt);
   // batched inverses of all diagonal blocks
   if (nt > 1)
-    issue_trtri(h, h->d_U, ns, ns, h->d_MF, 2 * ns + nd, (int)(nt - 1), ss, ns * (2 * ns + nd));
-  issue_trtri(h, h->d_U + (nt - 1) * ss, ns, ns, h->d_MF + mf_col_offset(sh, nt - 1), ns + nd, 1,
-              0, 0);
+    issue_trtri(h, h->d_U, ns, ns, h->d_MF, 2 * ns + nd, h->d_MS, 2 * ns + nd, (int)(nt - 1), ss,
+                ns * (2 * ns + nd), ns * (2 * ns + nd));
+  issue_trtri(h, h->d_U + (nt - 1) * ss, ns, ns, h->d_MF + mf_col_offset(sh, nt - 1), ns + nd,
+              h->d_MS + mf_col_offset(sh, nt - 1), ns + nd, 1, 0, 0, 0);
   if (nd > 0) {
-    issue_trtri(h, Ud, nd, nd, h->d_MF + mf_col_offset(sh, nt), nd, 1, 0, 0);
+    issue_trtri(h, Ud, nd, nd, h->d_MF + mf_col_offset(sh, nt), nd, Sdd, nd, 1, 0, 0, 0);
     // Sigma_dd = L_dd^{-T} L_dd^{-1} = U_d U_d^T   (RGF.H:439-442)
     gemm(h, mk(ind, ind, ind, Ud, nd, 0, Ud, nd, 1, nullptr, 0, Sdd, nd, 1.0, 0.0), SMALL);
   }
@@ -495,16 +552,26 @@ int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, F issue) {
 }
 
 int collect_timer(rgf_handle* h) {
-  for (size_t i = 0; i < h->ev_used.size(); ++i) {
+  for (const auto& t : h->ev_used) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, h->ev_used[i].first, h->ev_used[i].second);
-    h->timer_ms += ms;
-    h->timer_flops += h->ev_flops[i];
-    h->timer_launches++;
-    h->ev_pool.push_back(h->ev_used[i]);
+    cudaEventElapsedTime(&ms, t.e0, t.e1);
+    for (int k : {0, t.kind}) {
+      h->timer_ms[k] += ms;
+      h->timer_flops[k] += t.flops;
+      h->timer_launches[k]++;
+    }
+    h->timer_tflops += t.tensor_flops;
+    if (h->timer_detail_on) {
+      char key[128];
+      std::snprintf(key, sizeof(key), "%s cls%d m%5d n%5d k%5d b%4d", t.kind == 2 ? "split" : "fp64 ",
+                    t.cls, t.m, t.n, t.k, t.batch);
+      auto& e = h->timer_detail[key];
+      e.first++;
+      e.second += ms;
+    }
+    h->ev_pool.push_back({t.e0, t.e1});
   }
   h->ev_used.clear();
-  h->ev_flops.clear();
   return RGF_OK;
 }
 
@@ -570,12 +637,12 @@ void release(rgf_handle* h) {
   if (h->g_factor) cudaGraphExecDestroy(h->g_factor);
   if (h->g_selinv) cudaGraphExecDestroy(h->g_selinv);
   for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
-  for (auto& e : h->ev_used) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& e : h->ev_used) { cudaEventDestroy(e.e0); cudaEventDestroy(e.e1); }
   for (auto& e : h->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   delete h->split;
   void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
                   h->d_logpart, h->d_scalars, h->d_diag, h->d_status, h->d_rhs, h->d_partial,
-                  h->d_res};
+                  h->d_res, h->d_gemm_ws};
   for (void* p : bufs) dfree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -609,6 +676,7 @@ int rgf_default_opts(rgf_opts* o) {
   o->selinv_mode = RGF_SELINV_EXACT;
   o->device = -1;
   o->use_graphs = 1;
+  o->fp64_diag = 1;
   return RGF_OK;
 }
 
@@ -626,7 +694,8 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
   if (opts) o = *opts;
   if (o.precision != RGF_PREC_FP64 && o.precision != RGF_PREC_SPLIT) return RGF_EINVAL;
   if (o.selinv_mode != RGF_SELINV_EXACT && o.selinv_mode != RGF_SELINV_COMPAT) return RGF_EINVAL;
-  if (o.slices < 0 || o.slices > 16) return RGF_EINVAL;
+  if (o.slices < 0 || o.slices > 8) return RGF_EINVAL;
+  if (o.fp64_diag < 0 || o.fp64_diag > 2) return RGF_EINVAL;
 
   int dev = o.device;
   if (dev < 0) {
@@ -656,12 +725,19 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     if ((st = dalloc(h, &h->d_ja, h->nnz))) break;
     if ((st = dalloc(h, &h->d_a, h->nnz))) break;
     if ((st = dalloc(h, &h->d_MF, h->mf_size))) break;
-    const int tiles = (int)((ns + NB - 1) / NB), dtiles = (int)((nd + NB - 1) / NB);
+    if (const char* e = std::getenv("RGF_GB300_LEAF_NB")) {
+      const int v = std::atoi(e);
+      if (v == 16 || v == 32 || v == 64) h->nb = v;
+    }
+    const int tiles = (int)((ns + h->nb - 1) / h->nb), dtiles = (int)((nd + h->nb - 1) / h->nb);
     h->nparts = (int)(nt * tiles + dtiles);
     if ((st = dalloc(h, &h->d_logpart, h->nparts))) break;
     if ((st = dalloc(h, &h->d_scalars, 8))) break;
     if ((st = dalloc(h, &h->d_diag, n))) break;
     if ((st = dalloc(h, &h->d_status, 1))) break;
+    h->gemm_ws_elems = std::min<long long>(20ll << 20, 16ll * (2 * (long long)ns + (long long)nd) *
+                                                           std::max<long long>(ns, nd));
+    if ((st = dalloc(h, &h->d_gemm_ws, h->gemm_ws_elems))) break;
     if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice, h->stream) ||
         cudaMemcpyAsync(h->d_ja, ja, sizeof(size_t) * h->nnz, cudaMemcpyHostToDevice, h->stream) ||
         cudaMemcpyAsync(h->d_a, a, sizeof(double) * h->nnz, cudaMemcpyHostToDevice, h->stream)) {
@@ -837,19 +913,37 @@ int rgf_get_stream(rgf_handle* h, void** stream) {
 int rgf_kernel_timer_enable(rgf_handle* h, int enable) {
   if (!h) return RGF_EINVAL;
   h->timer_on = enable != 0;
+  h->timer_detail_on = enable > 1;
   return RGF_OK;
 }
 
-int rgf_kernel_timer_read(rgf_handle* h, int reset, double* ms, long long* launches,
+int rgf_kernel_timer_read(rgf_handle* h, int reset, int kind, double* ms, long long* launches,
                           double* flops) {
-  if (!h) return RGF_EINVAL;
-  if (ms) *ms = h->timer_ms;
-  if (launches) *launches = h->timer_launches;
-  if (flops) *flops = h->timer_flops;
+  if (!h || kind < 0 || kind > 3) return RGF_EINVAL;
+  const int k = kind == 3 ? 2 : kind;
+  if (ms) *ms = h->timer_ms[k];
+  if (launches) *launches = h->timer_launches[k];
+  if (flops) *flops = kind == 3 ? h->timer_tflops : h->timer_flops[k];
+  if (reset && h->timer_detail_on && !h->timer_detail.empty()) {
+    std::vector<std::pair<double, std::string>> rows;
+    for (auto& kv : h->timer_detail) {
+      char line[200];
+      std::snprintf(line, sizeof(line), "%s  x%6lld  %9.3f ms", kv.first.c_str(), kv.second.first,
+                    kv.second.second);
+      rows.push_back({kv.second.second, line});
+    }
+    std::sort(rows.rbegin(), rows.rend());
+    std::fprintf(stderr, "[rgf timer] per GEMM shape (top 40)\n");
+    for (size_t i = 0; i < rows.size() && i < 40; ++i) std::fprintf(stderr, "  %s\n", rows[i].second.c_str());
+    h->timer_detail.clear();
+  }
   if (reset) {
-    h->timer_ms = 0.0;
-    h->timer_flops = 0.0;
-    h->timer_launches = 0;
+    for (int i = 0; i < 3; ++i) {
+      h->timer_ms[i] = 0.0;
+      h->timer_flops[i] = 0.0;
+      h->timer_launches[i] = 0;
+    }
+    h->timer_tflops = 0.0;
   }
   return RGF_OK;
 }

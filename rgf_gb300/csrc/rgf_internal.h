@@ -32,6 +32,12 @@ struct GemmDesc {
   int triA = TRI_NONE, triB = TRI_NONE, outLower = 0;
   int batch = 1;
   long long sA = 0, sB = 0, sC = 0, sD = 0;
+  // FP64 kernel only: workspace for split-K partial sums (used when a single
+  // problem has too few output tiles to fill the GPU); ksplit is set by the
+  // launcher.
+  double* ws = nullptr;
+  long long ws_elems = 0;
+  int ksplit = 1;
 };
 
 // Algorithmic flops of one GemmDesc (triangular operands and lower-only
@@ -39,7 +45,8 @@ struct GemmDesc {
 double gemm_flops(const GemmDesc& g);
 
 // ---- FP64 kernels (k_fp64.cu) ---------------------------------------------
-void launch_gemm_fp64(const GemmDesc& g, cudaStream_t s);
+// Returns the number of kernels launched (2 with split-K).
+int launch_gemm_fp64(const GemmDesc& g, cudaStream_t s);
 
 // Cholesky of the nbk x nbk (nbk <= 64) lower tile at T (column-major, ldt),
 // in place.  Writes sum(log diag) of the tile to *logpart and records the

@@ -18,13 +18,16 @@ class SplitEngine {
   // Size the slice workspace for operands of up to max_rows rows and max_k
   // terms (allocates once, outside any graph capture).
   int prepare(int max_rows, int max_k);
-  // True when g can run on the tensor cores (single problem, k >= min_k and
-  // within the prepared sizes).
+  // True when g can run on the tensor cores (k >= min_k and within the
+  // prepared sizes; batched problems run in chunks that fit the workspace).
   bool supports(const GemmDesc& g) const;
   int slices() const { return slices_; }
   int min_k() const { return min_k_; }
-  // Issue D = alpha op(A) op(B) + beta C on stream s; returns kernels launched.
-  long long gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st);
+  // Issue D = alpha op(A) op(B) + beta C on stream s; returns kernels launched
+  // and, in *tensor_flops (if given), the bf16 slice-product flops it runs.
+  // slices > 0 overrides the engine's slice count (up to 8) for this call.
+  long long gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
+                 double* tensor_flops = nullptr, int slices = 0);
 
  private:
   SplitEngine() = default;

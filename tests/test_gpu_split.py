@@ -78,8 +78,15 @@ def test_split_gemm_scaled_rows_and_beta_zero(rgf):
     assert np.max(np.abs(got - ref) / bound) <= GEMM_TOL
 
 
+def test_split_gemm_eight_slices_is_fp64_accurate(rgf):
+    """8 slices (56-bit operands) reach the accuracy of an FP64 GEMM."""
+    out, ref, bound = _gemm_case(rgf, "N", "T", 640, 384, 1500, 1.0, 0.0, seed=3, slices=8)
+    assert np.max(np.abs(out["split"] - ref) / bound) <= 1e-15
+    assert np.max(np.abs(out["split"] - ref) / bound) <= 4 * np.max(np.abs(out["fp64"] - ref) / bound) + 1e-16
+
+
 @pytest.mark.parametrize("ns,nt,nd,fp64_diag", [
-    (300, 3, 2, True), (300, 3, 0, False), (520, 4, 4, True), (520, 4, 4, False),
+    (300, 3, 2, 1), (300, 3, 0, 0), (520, 4, 4, 1), (520, 4, 4, 0), (200, 5, 3, "native"),
 ])
 def test_split_solver_parity(rgf, ns, nt, nd, fp64_diag):
     ia, ja, a = gen.generate_bta(ns, nt, nd, seed=4)
