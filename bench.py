@@ -185,6 +185,78 @@ def run_reference(args, w):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """BASELINE's batched configuration: 256 uneven instances (ns in
+    {42,128,256,512}, nt in [3,60], nd in {0,2,6}, seed 4), factorize + logDet
+    + RGFdiag of all of them as one captured CUDA graph with a concurrent
+    branch per instance, against the same work launched instance by instance."""
+    import torch
+    import rgf_gb300
+    from rgf_gb300 import gen
+    from rgf_gb300.flops import algorithmic_flops
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    t = time.time()
+    inst = gen.generate_batch(args.batch_count, seed=4)
+    log(f"[bench] generated {len(inst)} instances in {time.time() - t:.1f}s")
+    flops = sum(algorithmic_flops(ns, nt, nd)["total"] for (_, _, _, ns, nt, nd) in inst)
+    b = rgf_gb300.RGFBatch(inst, precision=args.precision, slices=args.slices,
+                           device=torch.cuda.current_device(),
+                           fp64_diag=not args.no_fp64_diag)
+    stream = torch.cuda.ExternalStream(b.stream())
+    for _ in range(args.warmup):
+        b.run(concurrent=True, want_diag=False)
+    k0 = b.kernels()
+    clocks = Clocks(torch.cuda.current_device())
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run(concurrent=True, want_diag=False)
+    e1.record(stream); e1.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = (b.kernels() - k0) // args.steps
+    # per-instance launches (each instance's own stage graphs, one after another)
+    b.run(concurrent=False, want_diag=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run(concurrent=False, want_diag=False)
+    ms_serial = (time.perf_counter() - t0) * 1e3
+    # end to end: host CSC -> device for every instance, diag back to host
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b2 = rgf_gb300.RGFBatch(inst, precision=args.precision, slices=args.slices,
+                            device=torch.cuda.current_device(), fp64_diag=not args.no_fp64_diag)
+    _, diags = b2.run(concurrent=True, want_diag=True)
+    b2.close()
+    ms_e2e = (time.perf_counter() - t0) * 1e3
+    h2d = sum(x[0].nbytes + x[1].nbytes + x[2].nbytes for x in inst)
+    d2h = sum(d.nbytes for d in diags) + 8 * len(inst)
+    b.close()
+    if rank == 0:
+        line = {"metric": METRIC + f" over {len(inst)} uneven instances", "value": flops / (ms * 1e-3) / 1e12,
+                "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "bf16-slices/f64",
+                "data": "synthetic",
+                "config": {"workload": "batch", "count": len(inst), "seed": 4,
+                           "ns_choices": [42, 128, 256, 512], "nt_range": [3, 60],
+                           "nd_choices": [0, 2, 6], "precision": args.precision,
+                           "execution": "one captured CUDA graph, one concurrent branch per instance",
+                           "l2": "inputs larger than L2 (%.1f GB CSC)" % (h2d / 1e9)},
+                "per_instance_launches": {"value": flops / (ms_serial * 1e-3) / 1e12,
+                                          "ms_per_step": ms_serial},
+                "speedup_vs_per_instance": ms_serial / ms,
+                "e2e": {"value": flops / (ms_e2e * 1e-3) / 1e12, "unit": "TFLOP/s",
+                        "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def cfg_of(w):
     return {"ns": w["ns"], "nt": w["nt"], "nd": w["nd"], "seed": w["seed"],
             "spde_grid": w["spde"], "parallelism": "replicas"}
@@ -308,6 +380,28 @@ def run_rgf(args, w):
                     "kernel_share_of_step": fp["ms"] / ms_total}
     roofline["kernels"] = kernels
 
+    # plain FP64 on the same matrix for comparison (speed-up and accuracy)
+    plain = None
+    if args.precision == "split" and not args.no_fp64_ref:
+        s.close()
+        f = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision="fp64", device=dev)
+        f.factorize(); f.logDet(); d64 = f.RGFdiag()
+        fs = torch.cuda.ExternalStream(f.stream())
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True); p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(fs)
+        f.factorize(); ld64 = f.logDet(); f.diag_device_ptr()
+        p1.record(fs); p1.synchronize()
+        pms = p0.elapsed_time(p1)
+        f.close()
+        s = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
+                          slices=args.slices, device=dev, fp64_diag=not args.no_fp64_diag)
+        dsp = s.RGFdiag()
+        plain = {"value": flops / (pms * 1e-3) / 1e12, "ms_per_step": pms, "steps": 1, "warmup": 1,
+                 "speedup_of_split": pms / ms_step,
+                 "split_vs_fp64": {"logdet_rel": abs(logdet - ld64) / abs(ld64),
+                                   "diag_max_rel": float(np.max(np.abs(dsp - d64) / np.abs(d64)))}}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         tf, cores, sample, dt = cpu_port_sample(w, target_s=args.ref_seconds)
@@ -327,6 +421,7 @@ def run_rgf(args, w):
                          "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
+                "plain_fp64": plain,
                 "clocks": clk, "logdet": logdet,
                 "timed_region": "kernel timer on (events around each bulk GEMM launch), no graphs"}
         print(json.dumps(line), flush=True)
@@ -342,8 +437,11 @@ def main():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["rgf", "reference"], default="rgf")
-    p.add_argument("--workload", choices=sorted(WORKLOADS), default="ns2000_nt100_nd6")
-    p.add_argument("--precision", choices=["fp64", "split"], default="fp64")
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="ns2000_nt100_nd6")
+    p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--precision", choices=["fp64", "split"], default="split")
+    p.add_argument("--no-fp64-ref", action="store_true",
+                   help="skip the plain-FP64 comparison run (1 warm-up + 1 step)")
     p.add_argument("--slices", type=int, default=0)
     p.add_argument("--no-fp64-diag", action="store_true",
                    help="split precision: also run the diagonal blocks' inner updates as split products")
@@ -351,6 +449,13 @@ def main():
     p.add_argument("--ref-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     args = p.parse_args()
+    if args.workload == "batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no "
+                              "reference counterpart (one instance per RGF object)"}))
+        else:
+            run_batch(args)
+        return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w)

@@ -188,6 +188,29 @@ int rgf_residual_norm_noalloc(size_t n, const size_t* d_ia, const size_t* d_ja,
                               const double* d_a, const double* d_x, const double* d_b,
                               double* d_out, void* stream);
 
+/* ---- batches of independent instances --------------------------------------
+ * Many factorizations of uneven (ns, nt, nd), as in a hyper-parameter search.
+ * The reference handles one instance per RGF object (RGF.H:84); a batch holds
+ * `count` instances, each created as by rgf_create from its own CSC. */
+typedef struct rgf_batch rgf_batch;
+
+int rgf_batch_create(size_t count, const size_t* const* ia, const size_t* const* ja,
+                     const double* const* a, const size_t* ns, const size_t* nt,
+                     const size_t* nd, const rgf_opts* opts, rgf_batch** out);
+int rgf_batch_destroy(rgf_batch* b);
+int rgf_batch_size(rgf_batch* b, size_t* count);
+/* Instance i as an ordinary handle (solve, export, ... ); owned by the batch. */
+int rgf_batch_handle(rgf_batch* b, size_t i, rgf_handle** h);
+int rgf_batch_get_stream(rgf_batch* b, void** stream);
+/* factorize + logDet + RGFdiag of every instance.  mode 0: one captured CUDA
+ * graph with one concurrent branch per instance (built on first use, then
+ * replayed with a single launch); mode 1: instance after instance, each with
+ * its own stage launches (the per-instance baseline).  logdet[count] and
+ * diag[i] (n_i doubles; diag or diag[i] may be NULL) receive the results. */
+int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag);
+/* GPU kernels launched by the batch's runs so far. */
+int rgf_batch_kernels(rgf_batch* b, long long* kernels);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-__all__ = ["RGF", "RGFError", "load_library", "library_path", "STATUS"]
+__all__ = ["RGF", "RGFBatch", "RGFError", "load_library", "library_path", "STATUS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
@@ -72,6 +72,15 @@ _SIGS = {
     "rgf_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "rgf_kernel_timer_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "rgf_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "rgf_batch_create": (C.c_int, [C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.POINTER(_Opts),
+                                   C.POINTER(C.c_void_p)]),
+    "rgf_batch_destroy": (C.c_int, [C.c_void_p]),
+    "rgf_batch_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "rgf_batch_handle": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
+    "rgf_batch_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rgf_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "rgf_batch_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "rgf_dgemm_device": (C.c_int, [C.c_int, C.c_int, C.c_char, C.c_char, C.c_int, C.c_int,
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p,
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
@@ -284,3 +293,77 @@ class RGF:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class RGFBatch:
+    """Many independent instances (uneven ns, nt, nd) factorized together.
+
+    ``instances`` is a sequence of ``(ia, ja, a, ns, nt, nd)``.  ``run()``
+    returns ``(logdet[count], [diag_0, ...])``: with ``concurrent=True`` the
+    whole batch is one captured CUDA graph with a concurrent branch per
+    instance; ``concurrent=False`` runs instance after instance (the
+    per-instance baseline).  Options are those of :class:`RGF`.
+    """
+
+    def __init__(self, instances, precision: str = "fp64", slices: int = 0,
+                 selinv: str = "exact", device: int = -1, fp64_diag=1):
+        lib = load_library()
+        self._lib = lib
+        self._h = C.c_void_p()
+        self._keep = []
+        cnt = len(instances)
+        ia_p = (C.c_void_p * cnt)()
+        ja_p = (C.c_void_p * cnt)()
+        a_p = (C.c_void_p * cnt)()
+        ns = np.empty(cnt, dtype=np.uint64)
+        nt = np.empty(cnt, dtype=np.uint64)
+        nd = np.empty(cnt, dtype=np.uint64)
+        self.sizes = []
+        for i, (ia, ja, a, s_, t_, d_) in enumerate(instances):
+            ia = np.ascontiguousarray(ia, dtype=np.uint64)
+            ja = np.ascontiguousarray(ja, dtype=np.uint64)
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            self._keep += [ia, ja, a]
+            ia_p[i], ja_p[i], a_p[i] = ia.ctypes.data, ja.ctypes.data, a.ctypes.data
+            ns[i], nt[i], nd[i] = s_, t_, d_
+            self.sizes.append((int(s_), int(t_), int(d_)))
+        o = _Opts()
+        lib.rgf_default_opts(C.byref(o))
+        o.precision = PRECISION[precision]
+        o.slices = int(slices)
+        o.selinv_mode = SELINV[selinv]
+        o.device = int(device)
+        o.fp64_diag = {True: 1, False: 0, "native": 2}.get(fp64_diag, fp64_diag)
+        _check(lib.rgf_batch_create(cnt, ia_p, ja_p, a_p, _ptr(ns), _ptr(nt), _ptr(nd),
+                                    C.byref(o), C.byref(self._h)), "rgf_batch_create")
+        self._keep = []  # the library copied the CSC to the device
+        self.count = cnt
+
+    def run(self, concurrent: bool = True, want_diag: bool = True):
+        logdet = np.empty(self.count, dtype=np.float64)
+        diags = [np.empty(s * t + d, dtype=np.float64) for (s, t, d) in self.sizes] if want_diag else []
+        ptrs = (C.c_void_p * self.count)(*[x.ctypes.data for x in diags]) if want_diag else None
+        _check(self._lib.rgf_batch_run(self._h, 0 if concurrent else 1, _ptr(logdet),
+                                       ptrs), "rgf_batch_run")
+        return logdet, diags
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.rgf_batch_get_stream(self._h, C.byref(p)), "rgf_batch_get_stream")
+        return p.value or 0
+
+    def kernels(self) -> int:
+        k = C.c_longlong()
+        _check(self._lib.rgf_batch_kernels(self._h, C.byref(k)), "rgf_batch_kernels")
+        return k.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.rgf_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -550,11 +550,14 @@ size_t item_bytes(int S, int RpA, int RpB, int Kp) {
 }
 }  // namespace
 
-int SplitEngine::reserve(int max_rows, int max_k) {
-  // one problem of the largest size at the largest slice count, and at least
-  // 1 GiB so that batched problems run in few chunks
+int SplitEngine::reserve(int max_rows, int max_k, int batch_hint) {
+  // one problem of the largest size at the largest slice count, plus room for
+  // a batch of half-size problems (the top level of the batched inverses),
+  // at most 1 GiB: larger batches run in chunks
   const size_t one = item_bytes(MAX_SLICES, max_rows, max_rows, max_k);
-  return ensure_ws(std::max(one, (size_t)1 << 30) + 1024);
+  const int h = round_up(std::max(max_k / 2, 1), BM);
+  const size_t batch = (size_t)std::max(batch_hint, 1) * item_bytes(MAX_SLICES, h, h, h);
+  return ensure_ws(std::max(one, std::min(batch, (size_t)1 << 30)) + 1024);
 }
 
 bool SplitEngine::supports(const GemmDesc& g) const {
@@ -563,10 +566,10 @@ bool SplitEngine::supports(const GemmDesc& g) const {
          round_up(g.k, BKE) <= max_k_;
 }
 
-int SplitEngine::prepare(int max_rows, int max_k) {
+int SplitEngine::prepare(int max_rows, int max_k, int batch_hint) {
   max_rows_ = round_up(std::max(max_rows, 1), BM);
   max_k_ = round_up(std::max(max_k, 1), BKE);
-  return reserve(max_rows_, max_k_);
+  return reserve(max_rows_, max_k_, batch_hint);
 }
 
 long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,

@@ -361,6 +361,10 @@ void issue_selinv(rgf_handle* h) {
   const long long ss = ns * ns;
   double* Ud = h->d_U + nt * ss;
   double* Sdd = h->d_MS + mf_col_offset(sh, nt);
+  // The inverses are upper triangular and are read below as full blocks
+  // (W^T = U_i - ...); the recursion writes only their upper part, so the
+  // strictly lower part must be zero.
+  cudaMemsetAsync(h->d_U, 0, sizeof(double) * (nt * ss + nd * nd), s);
   // batched inverses of all diagonal blocks
   if (nt > 1)
     issue_trtri(h, h->d_U, ns, ns, h->d_MF, 2 * ns + nd, h->d_MS, 2 * ns + nd, (int)(nt - 1), ss,
@@ -602,19 +606,24 @@ int ensure_factored(rgf_handle* h) {
   return RGF_OK;
 }
 
+int alloc_selinv(rgf_handle* h) {
+  if (h->d_MS) return RGF_OK;
+  const long long ns = h->sh.ns, nt = h->sh.nt, nd = h->sh.nd;
+  int st;
+  if ((st = dalloc(h, &h->d_MS, h->mf_size))) return st;
+  if ((st = dalloc(h, &h->d_U, nt * ns * ns + nd * nd))) return st;
+  if ((st = dalloc(h, &h->d_T1, ns * ns))) return st;
+  if ((st = dalloc(h, &h->d_T2, ns * ns))) return st;
+  if ((st = dalloc(h, &h->d_T3, std::max<long long>(1, nd * ns)))) return st;
+  RGF_CK(cudaMemsetAsync(h->d_MS, 0, sizeof(double) * h->mf_size, h->stream));
+  return RGF_OK;
+}
+
 int ensure_selinv(rgf_handle* h) {
   int st = ensure_factored(h);
   if (st) return st;
   if (h->selinv_done) return RGF_OK;
-  if (!h->d_MS) {
-    const long long ns = h->sh.ns, nt = h->sh.nt, nd = h->sh.nd;
-    if ((st = dalloc(h, &h->d_MS, h->mf_size))) return st;
-    if ((st = dalloc(h, &h->d_U, nt * ns * ns + nd * nd))) return st;
-    if ((st = dalloc(h, &h->d_T1, ns * ns))) return st;
-    if ((st = dalloc(h, &h->d_T2, ns * ns))) return st;
-    if ((st = dalloc(h, &h->d_T3, std::max<long long>(1, nd * ns)))) return st;
-    RGF_CK(cudaMemsetAsync(h->d_MS, 0, sizeof(double) * h->mf_size, h->stream));
-  }
+  if ((st = alloc_selinv(h))) return st;
   st = run_stage(h, &h->g_selinv, &h->k_selinv, [&] { issue_selinv(h); });
   if (st) return st;
   st = sync_and_check(h);
@@ -735,7 +744,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     if ((st = dalloc(h, &h->d_scalars, 8))) break;
     if ((st = dalloc(h, &h->d_diag, n))) break;
     if ((st = dalloc(h, &h->d_status, 1))) break;
-    h->gemm_ws_elems = std::min<long long>(20ll << 20, 16ll * (2 * (long long)ns + (long long)nd) *
+    h->gemm_ws_elems = std::min<long long>(20ll << 20, 8ll * (2 * (long long)ns + (long long)nd) *
                                                            std::max<long long>(ns, nd));
     if ((st = dalloc(h, &h->d_gemm_ws, h->gemm_ws_elems))) break;
     if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice, h->stream) ||
@@ -748,7 +757,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
       h->split = SplitEngine::create(o.slices, &st);
       if (st) break;
       // operands have at most 2ns+nd rows and ns (or nd) terms
-      st = h->split->prepare((int)(2 * ns + nd), (int)std::max(ns, nd));
+      st = h->split->prepare((int)(2 * ns + nd), (int)std::max(ns, nd), (int)nt);
       if (st) break;
     }
     // validate the pattern once on the device
@@ -994,6 +1003,169 @@ int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m,
 int rgf_measure_fp64_peak(double* tflops) {
   if (!tflops) return RGF_EINVAL;
   return measure_fp64_peak(tflops);
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Batches of independent instances (many factorizations of uneven (ns, nt, nd)
+// as in a hyper-parameter search).  Every instance keeps its own handle,
+// stream and workspaces; the whole batch's factorize + selected inversion is
+// captured once as ONE CUDA graph whose branches (one per instance) run
+// concurrently, and replayed with a single graph launch.
+// ============================================================================
+struct rgf_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<rgf_handle*> h;
+  std::vector<cudaEvent_t> ev;
+  cudaGraphExec_t g_all = nullptr;
+  long long k_all = 0;
+  long long kernels_total = 0;
+};
+
+namespace {
+
+void batch_release(rgf_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->g_all) cudaGraphExecDestroy(b->g_all);
+  for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
+  for (rgf_handle* h : b->h) release(h);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int batch_build_graph(rgf_batch* b) {
+  for (rgf_handle* h : b->h) {
+    int st = alloc_selinv(h);
+    if (st) return st;
+  }
+  RGF_CK(cudaStreamSynchronize(b->stream));
+  for (rgf_handle* h : b->h) RGF_CK(cudaStreamSynchronize(h->stream));
+  const size_t n = b->h.size();
+  if (b->ev.empty()) {
+    b->ev.resize(n + 1);
+    for (auto& e : b->ev) RGF_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  cudaGraph_t graph = nullptr;
+  RGF_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(b->ev[0], b->stream);
+  long long nk = 0;
+  for (size_t i = 0; i < n; ++i) {
+    rgf_handle* h = b->h[i];
+    cudaStreamWaitEvent(h->stream, b->ev[0], 0);
+    h->kernels_issued = 0;
+    issue_factor(h);
+    issue_selinv(h);
+    nk += h->kernels_issued;
+    cudaEventRecord(b->ev[i + 1], h->stream);
+    cudaStreamWaitEvent(b->stream, b->ev[i + 1], 0);
+  }
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaGraphInstantiate(&b->g_all, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    b->g_all = nullptr;
+    return cuda_status(e);
+  }
+  b->k_all = nk;
+  return RGF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rgf_batch_create(size_t count, const size_t* const* ia, const size_t* const* ja,
+                     const double* const* a, const size_t* ns, const size_t* nt, const size_t* nd,
+                     const rgf_opts* opts, rgf_batch** out) {
+  if (!out || count == 0 || !ia || !ja || !a || !ns || !nt || !nd) return RGF_EINVAL;
+  *out = nullptr;
+  rgf_batch* b = new (std::nothrow) rgf_batch();
+  if (!b) return RGF_ENOMEM;
+  int st = RGF_OK;
+  for (size_t i = 0; i < count && !st; ++i) {
+    rgf_handle* h = nullptr;
+    st = rgf_create(ia[i], ja[i], a[i], ns[i], nt[i], nd[i], opts, &h);
+    if (!st) b->h.push_back(h);
+  }
+  if (!st) {
+    b->device = b->h[0]->device;
+    cudaSetDevice(b->device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) st = RGF_ECUDA;
+  }
+  if (st) {
+    batch_release(b);
+    return st;
+  }
+  *out = b;
+  return RGF_OK;
+}
+
+int rgf_batch_destroy(rgf_batch* b) {
+  if (!b) return RGF_EINVAL;
+  batch_release(b);
+  return RGF_OK;
+}
+
+int rgf_batch_size(rgf_batch* b, size_t* count) {
+  if (!b || !count) return RGF_EINVAL;
+  *count = b->h.size();
+  return RGF_OK;
+}
+
+int rgf_batch_handle(rgf_batch* b, size_t i, rgf_handle** h) {
+  if (!b || !h || i >= b->h.size()) return RGF_EINVAL;
+  *h = b->h[i];
+  return RGF_OK;
+}
+
+int rgf_batch_get_stream(rgf_batch* b, void** stream) {
+  if (!b || !stream) return RGF_EINVAL;
+  *stream = (void*)b->stream;
+  return RGF_OK;
+}
+
+int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag) {
+  if (!b || (mode != 0 && mode != 1)) return RGF_EINVAL;
+  if (cudaSetDevice(b->device) != cudaSuccess) return RGF_ECUDA;
+  int st = RGF_OK;
+  if (mode == 0) {
+    if (!b->g_all && (st = batch_build_graph(b))) return st;
+    RGF_CK(cudaGraphLaunch(b->g_all, b->stream));
+    RGF_CK(cudaStreamSynchronize(b->stream));
+    b->kernels_total += b->k_all;
+    for (rgf_handle* h : b->h) {
+      h->factored = false;
+      h->selinv_done = false;
+      if ((st = sync_and_check(h))) return st;
+      h->factored = true;
+      h->selinv_done = true;
+    }
+  } else {
+    for (rgf_handle* h : b->h) {
+      const long long k0 = h->kernels_total;
+      if ((st = rgf_factorize(h))) return st;
+      if ((st = ensure_selinv(h))) return st;
+      b->kernels_total += h->kernels_total - k0;
+    }
+  }
+  for (size_t i = 0; i < b->h.size(); ++i) {
+    rgf_handle* h = b->h[i];
+    if (logdet) RGF_CK(cudaMemcpy(&logdet[i], h->d_scalars, sizeof(double), cudaMemcpyDeviceToHost));
+    if (diag && diag[i])
+      RGF_CK(cudaMemcpy(diag[i], h->d_diag, sizeof(double) * h->sh.n, cudaMemcpyDeviceToHost));
+  }
+  return RGF_OK;
+}
+
+int rgf_batch_kernels(rgf_batch* b, long long* kernels) {
+  if (!b || !kernels) return RGF_EINVAL;
+  *kernels = b->kernels_total;
+  return RGF_OK;
 }
 
 }  // extern "C"

@@ -17,7 +17,9 @@ class SplitEngine {
   ~SplitEngine();
   // Size the slice workspace for operands of up to max_rows rows and max_k
   // terms (allocates once, outside any graph capture).
-  int prepare(int max_rows, int max_k);
+  // batch_hint: largest batch the caller issues (sizes the workspace so that
+  // batched problems run in few chunks; capped at 1 GiB).
+  int prepare(int max_rows, int max_k, int batch_hint = 1);
   // True when g can run on the tensor cores (k >= min_k and within the
   // prepared sizes; batched problems run in chunks that fit the workspace).
   bool supports(const GemmDesc& g) const;
@@ -32,7 +34,7 @@ class SplitEngine {
  private:
   SplitEngine() = default;
   int ensure_ws(size_t bytes);
-  int reserve(int max_rows, int max_k);
+  int reserve(int max_rows, int max_k, int batch_hint);
   int slices_ = 0;
   int min_k_ = 1 << 30;
   int max_rows_ = 0, max_k_ = 0;

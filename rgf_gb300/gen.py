@@ -137,3 +137,21 @@ def write_rhs(path, b) -> None:
     """RHS file read by main.C:79-84 (one value per line, column-major)."""
     with open(path, "w") as f:
         f.write("\n".join(repr(float(v)) for v in np.asarray(b).ravel(order="F")) + "\n")
+
+
+def batch_shapes(count: int, seed: int, ns_choices=(42, 128, 256, 512), nt_range=(3, 60),
+                 nd_choices=(0, 2, 6)):
+    """Seeded uneven instance sizes: ns from ns_choices, nt uniform in
+    nt_range (inclusive), nd from nd_choices."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.choice(ns_choices)), int(rng.integers(nt_range[0], nt_range[1] + 1)),
+             int(rng.choice(nd_choices))) for _ in range(count)]
+
+
+def generate_batch(count: int, seed: int, **kw):
+    """(ia, ja, a, ns, nt, nd) for `count` seeded uneven instances."""
+    out = []
+    for i, (ns, nt, nd) in enumerate(batch_shapes(count, seed, **kw)):
+        ia, ja, a = generate_bta(ns, nt, nd, seed * 100003 + i)
+        out.append((ia, ja, a, ns, nt, nd))
+    return out
