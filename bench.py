@@ -257,6 +257,131 @@ def run_batch(args):
         print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """BASELINE's serving configuration: Poisson arrivals at --rate req/s,
+    70% new factorize+logDet, 20% solve (1-16 RHS) on a resident factor, 10%
+    RGFdiag on a resident factor; ns from {42,128,256,512,1024,1500}, nt in
+    [3,100], nd in [0,6].  Requests are admitted by HBM footprint into a
+    continuous-batching loop.  Reports p50/p99 latency and throughput for the
+    chosen precision and for plain FP64, and the logDet error of split against
+    FP64 on the same matrices."""
+    import threading
+    import torch
+    import rgf_gb300
+    from rgf_gb300 import gen
+    from rgf_gb300.flops import algorithmic_flops
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(5)
+    pool_shapes = [(int(rng.choice([42, 128, 256, 512, 1024, 1500])), int(rng.integers(3, 101)),
+                    int(rng.integers(0, 7))) for _ in range(args.serve_pool)]
+    t0 = time.time()
+    pool = [gen.generate_bta(ns, nt, nd, 5000 + i) for i, (ns, nt, nd) in enumerate(pool_shapes)]
+    log(f"[bench] generated {len(pool)} serving matrices in {time.time() - t0:.1f}s")
+    nreq = args.serve_requests
+    kinds0 = rng.choice([0, 1, 2], size=nreq, p=[0.7, 0.2, 0.1])
+    kinds0[0] = 0
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=nreq))
+    mats0 = rng.integers(0, len(pool), size=nreq)
+    nrhs = rng.integers(1, 17, size=nreq)
+
+    def one_run(precision):
+        kinds = kinds0.copy()
+        mats = mats0.copy()
+        rng = np.random.default_rng(6)
+        srv = rgf_gb300.RGFServer(hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
+                                  slots=args.serve_slots, precision=precision)
+        resident = []          # (factor_id, pool index) of completed factorizations
+        lock = threading.Lock()
+        results = [None] * nreq
+        tickets = []
+
+        def waiter():
+            for (i, t) in iter(tickets_q.get, None):
+                r = srv.wait(t)
+                results[i] = r
+                if r["kind"] == 0 and r["status"] == 0:
+                    with lock:
+                        resident.append((r["factor_id"], int(mats[i])))
+
+        import queue as _q
+        tickets_q = _q.Queue()
+        th = [threading.Thread(target=waiter) for _ in range(4)]
+        for t in th:
+            t.start()
+        start = time.perf_counter()
+        flops = 0.0
+        for i in range(nreq):
+            delay = arrivals[i] - (time.perf_counter() - start)
+            if delay > 0:
+                time.sleep(delay)
+            kind = int(kinds[i])
+            with lock:
+                have = list(resident[-16:])
+            if kind != 0 and not have:
+                kind = 0
+            if kind == 0:
+                ns, nt, nd = pool_shapes[mats[i]]
+                t = srv.submit_factor(*pool[mats[i]], ns, nt, nd)
+                flops += algorithmic_flops(ns, nt, nd)["factor"]
+            else:
+                fid, pi = have[int(rng.integers(0, len(have)))]
+                mats[i] = pi
+                ns, nt, nd = pool_shapes[pi]
+                n = ns * nt + nd
+                if kind == 1:
+                    t = srv.submit_solve(fid, rng.standard_normal((n, int(nrhs[i]))))
+                else:
+                    t = srv.submit_diag(fid, n)
+                    flops += algorithmic_flops(ns, nt, nd)["selinv"]
+            kinds[i] = kind
+            tickets_q.put((i, t))
+        for _ in th:
+            tickets_q.put(None)
+        for t in th:
+            t.join()
+        makespan = time.perf_counter() - start
+        stats = srv.stats()
+        srv.close()
+        lat = np.array([r["latency_ms"] for r in results if r and r["status"] == 0])
+        ok = sum(1 for r in results if r and r["status"] == 0)
+        by = {}
+        for k, name in ((0, "factor"), (1, "solve"), (2, "diag")):
+            l = np.array([r["latency_ms"] for i, r in enumerate(results)
+                          if r and r["status"] == 0 and kinds[i] == k])
+            nfail = sum(1 for i, r in enumerate(results) if r and r["status"] != 0 and kinds[i] == k)
+            if l.size or nfail:
+                by[name] = {"count": int(l.size), "failed": nfail}
+            if l.size:
+                by[name].update(p50_ms=float(np.percentile(l, 50)),
+                                p99_ms=float(np.percentile(l, 99)))
+        logdets = {int(mats[i]): r["logdet"] for i, r in enumerate(results)
+                   if r and r["status"] == 0 and kinds[i] == 0}
+        return {"requests": nreq, "completed_ok": ok, "makespan_s": makespan,
+                "throughput_req_s": ok / makespan,
+                "fp64_equiv_tflops": flops / makespan / 1e12,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "by_kind": by, "evicted": stats["evicted"], "failed": stats["failed"]}, logdets
+
+    split, ld_s = one_run(args.precision)
+    plain, ld_p = one_run("fp64")
+    common = [k for k in ld_s if k in ld_p]
+    err = max((abs(ld_s[k] - ld_p[k]) / abs(ld_p[k]) for k in common), default=None)
+    line = {"metric": "serve p50/p99 latency and throughput (Poisson %.0f req/s)" % args.rate,
+            "value": split["p99_ms"], "unit": "ms (p99)", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": split["makespan_s"] * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16-slices/f64" if args.precision == "split" else "f64",
+            "data": "synthetic",
+            "config": {"workload": "serve", "rate_req_s": args.rate, "requests": nreq,
+                       "mix": {"factor+logdet": 0.7, "solve (1-16 RHS)": 0.2, "rgfdiag": 0.1},
+                       "ns_choices": [42, 128, 256, 512, 1024, 1500], "nt_range": [3, 100],
+                       "nd_range": [0, 6], "matrix_pool": len(pool), "slots": args.serve_slots,
+                       "hbm_budget_gb": args.serve_budget_gb},
+            args.precision: split, "fp64": plain,
+            "logdet_rel_err_split_vs_fp64": err}
+    print(json.dumps(line), flush=True)
+
+
 def cfg_of(w):
     return {"ns": w["ns"], "nt": w["nt"], "nd": w["nd"], "seed": w["seed"],
             "spde_grid": w["spde"], "parallelism": "replicas"}
@@ -437,7 +562,13 @@ def main():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["rgf", "reference"], default="rgf")
-    p.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch"], default="ns2000_nt100_nd6")
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "serve"],
+                   default="ns2000_nt100_nd6")
+    p.add_argument("--rate", type=float, default=2000.0)
+    p.add_argument("--serve-requests", type=int, default=400)
+    p.add_argument("--serve-pool", type=int, default=24)
+    p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--serve-budget-gb", type=float, default=160.0)
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--precision", choices=["fp64", "split"], default="split")
     p.add_argument("--no-fp64-ref", action="store_true",
@@ -449,6 +580,13 @@ def main():
     p.add_argument("--ref-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     args = p.parse_args()
+    if args.workload == "serve":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no request "
+                              "loop (one synchronous instance per RGF object)"}))
+        else:
+            run_serve(args)
+        return
     if args.workload == "batch":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no "

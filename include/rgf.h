@@ -211,6 +211,57 @@ int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag);
 /* GPU kernels launched by the batch's runs so far. */
 int rgf_batch_kernels(rgf_batch* b, long long* kernels);
 
+/* ---- request loop (serving) -------------------------------------------------
+ * Continuous batching on one GPU: `slots` workers take requests as soon as
+ * they are free and, for a new factorization, as soon as its HBM footprint
+ * fits `hbm_budget_bytes` (least-recently-used idle factors are evicted to make
+ * room); admitted requests run concurrently on their own streams.  Factors
+ * stay resident for follow-up solve / RGFdiag requests until released or
+ * evicted.  Built on the lazy-factorize, resident-factor semantics of the
+ * class (RGF.H:561, 585, 619); the reference has no request loop. */
+enum rgf_request_kind {
+  RGF_REQ_FACTOR = 0,   /* create + factorize + logDet; returns factor_id    */
+  RGF_REQ_SOLVE = 1,    /* x = A^{-1} b with a resident factor              */
+  RGF_REQ_DIAG = 2,     /* diag(A^{-1}) with a resident factor              */
+  RGF_REQ_RELEASE = 3   /* drop a resident factor                           */
+};
+
+/* Caller-owned; every pointer it holds must stay valid until the request is
+ * done.  The server writes factor_id (FACTOR), logdet, status and latency. */
+typedef struct rgf_request {
+  int kind;
+  int status;            /* out: rgf_status, -1 while pending                */
+  long long factor_id;   /* in: SOLVE/DIAG/RELEASE; out: FACTOR               */
+  const size_t* ia;      /* FACTOR: lower CSC and sizes                        */
+  const size_t* ja;
+  const double* a;
+  size_t ns, nt, nd;
+  const double* b;       /* SOLVE: n x nrhs column-major                       */
+  double* x;
+  size_t nrhs;
+  double* diag;          /* DIAG: n doubles                                    */
+  double logdet;         /* out: FACTOR                                        */
+  double latency_ms;     /* out: submit to completion                          */
+  size_t reserved_bytes; /* internal                                           */
+} rgf_request;
+
+typedef struct rgf_server_stats_t {
+  long long submitted, admitted, completed, failed, evicted;
+  long long resident_factors, queued;
+  size_t used_bytes;
+} rgf_server_stats_t;
+
+typedef struct rgf_server rgf_server;
+int rgf_server_create(const rgf_opts* opts, size_t hbm_budget_bytes, int slots,
+                      rgf_server** out);
+int rgf_server_submit(rgf_server* s, rgf_request* req, long long* ticket);
+/* Wait up to timeout_s for a ticket; *status receives the request's status.
+ * Returns RGF_ETIMEOUT if it is still running. */
+int rgf_server_wait(rgf_server* s, long long ticket, double timeout_s, int* status);
+int rgf_server_stats(rgf_server* s, rgf_server_stats_t* stats);
+/* Stops the workers (requests still queued are not run) and frees factors. */
+int rgf_server_destroy(rgf_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,8 @@ import os
 
 import numpy as np
 
-__all__ = ["RGF", "RGFBatch", "RGFError", "load_library", "library_path", "STATUS"]
+__all__ = ["RGF", "RGFBatch", "RGFServer", "RGFError", "load_library", "library_path",
+           "STATUS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
@@ -46,6 +47,22 @@ class _Info(C.Structure):
                 ("device_bytes", C.c_size_t), ("not_spd_column", C.c_int),
                 ("reserved0", C.c_int), ("kernels_launched", C.c_longlong),
                 ("reserved", C.c_int * 4)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("status", C.c_int), ("factor_id", C.c_longlong),
+                ("ia", C.c_void_p), ("ja", C.c_void_p), ("a", C.c_void_p),
+                ("ns", C.c_size_t), ("nt", C.c_size_t), ("nd", C.c_size_t),
+                ("b", C.c_void_p), ("x", C.c_void_p), ("nrhs", C.c_size_t),
+                ("diag", C.c_void_p), ("logdet", C.c_double), ("latency_ms", C.c_double),
+                ("reserved_bytes", C.c_size_t)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong),
+                ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("evicted", C.c_longlong), ("resident_factors", C.c_longlong),
+                ("queued", C.c_longlong), ("used_bytes", C.c_size_t)]
 
 
 def library_path() -> str:
@@ -81,6 +98,11 @@ _SIGS = {
     "rgf_batch_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "rgf_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "rgf_batch_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "rgf_server_create": (C.c_int, [C.POINTER(_Opts), C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
+    "rgf_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong)]),
+    "rgf_server_wait": (C.c_int, [C.c_void_p, C.c_longlong, C.c_double, C.POINTER(C.c_int)]),
+    "rgf_server_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rgf_server_destroy": (C.c_int, [C.c_void_p]),
     "rgf_dgemm_device": (C.c_int, [C.c_int, C.c_int, C.c_char, C.c_char, C.c_int, C.c_int,
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p,
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
@@ -360,6 +382,94 @@ class RGFBatch:
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
             self._lib.rgf_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RGFServer:
+    """Request loop with continuous batching and resident factors.
+
+    ``submit_factor`` / ``submit_solve`` / ``submit_diag`` / ``submit_release``
+    return a ticket; ``wait(ticket)`` returns a dict with the request's
+    status, latency and results (``factor_id`` and ``logdet`` for factor
+    requests, ``x`` for solves, ``diag`` for RGFdiag).
+    """
+
+    FACTOR, SOLVE, DIAG, RELEASE = 0, 1, 2, 3
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 8, precision: str = "fp64",
+                 slices: int = 0, selinv: str = "exact", device: int = -1, fp64_diag=1):
+        lib = load_library()
+        self._lib = lib
+        self._h = C.c_void_p()
+        o = _Opts()
+        lib.rgf_default_opts(C.byref(o))
+        o.precision = PRECISION[precision]
+        o.slices = int(slices)
+        o.selinv_mode = SELINV[selinv]
+        o.device = int(device)
+        o.fp64_diag = {True: 1, False: 0, "native": 2}.get(fp64_diag, fp64_diag)
+        _check(lib.rgf_server_create(C.byref(o), int(hbm_budget_bytes), int(slots),
+                                     C.byref(self._h)), "rgf_server_create")
+        self._live = {}
+
+    def _submit(self, req, keep):
+        t = C.c_longlong()
+        _check(self._lib.rgf_server_submit(self._h, C.byref(req), C.byref(t)), "rgf_server_submit")
+        self._live[t.value] = (req, keep)
+        return t.value
+
+    def submit_factor(self, ia, ja, a, ns, nt, nd) -> int:
+        ia = np.ascontiguousarray(ia, dtype=np.uint64)
+        ja = np.ascontiguousarray(ja, dtype=np.uint64)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        r = _Request(kind=self.FACTOR, ia=ia.ctypes.data, ja=ja.ctypes.data, a=a.ctypes.data,
+                     ns=ns, nt=nt, nd=nd)
+        return self._submit(r, {"ia": ia, "ja": ja, "a": a})
+
+    def submit_solve(self, factor_id: int, b) -> int:
+        b = np.asfortranarray(b, dtype=np.float64)
+        if b.ndim == 1:
+            b = b.reshape(-1, 1, order="F")
+        x = np.empty_like(b, order="F")
+        r = _Request(kind=self.SOLVE, factor_id=factor_id, b=b.ctypes.data, x=x.ctypes.data,
+                     nrhs=b.shape[1])
+        return self._submit(r, {"b": b, "x": x})
+
+    def submit_diag(self, factor_id: int, n: int) -> int:
+        d = np.empty(n, dtype=np.float64)
+        r = _Request(kind=self.DIAG, factor_id=factor_id, diag=d.ctypes.data)
+        return self._submit(r, {"diag": d})
+
+    def submit_release(self, factor_id: int) -> int:
+        return self._submit(_Request(kind=self.RELEASE, factor_id=factor_id), {})
+
+    def wait(self, ticket: int, timeout_s: float = 600.0) -> dict:
+        st = C.c_int()
+        _check(self._lib.rgf_server_wait(self._h, ticket, timeout_s, C.byref(st)), "rgf_server_wait")
+        req, keep = self._live.pop(ticket)
+        out = {"status": req.status, "latency_ms": req.latency_ms, "kind": req.kind}
+        if req.kind == self.FACTOR:
+            out.update(factor_id=req.factor_id, logdet=req.logdet)
+        if "x" in keep:
+            out["x"] = keep["x"]
+        if "diag" in keep:
+            out["diag"] = keep["diag"]
+        return out
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(self._lib.rgf_server_stats(self._h, C.byref(st)), "rgf_server_stats")
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.rgf_server_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):
