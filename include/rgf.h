@@ -217,7 +217,9 @@ int rgf_batch_kernels(rgf_batch* b, long long* kernels);
  * fits `hbm_budget_bytes` (least-recently-used idle factors are evicted to make
  * room); admitted requests run concurrently on their own streams.  Factors
  * stay resident for follow-up solve / RGFdiag requests until released or
- * evicted.  Built on the lazy-factorize, resident-factor semantics of the
+ * evicted; a factor that a submitted, not yet run request names is never
+ * evicted, so such a request fails only if the factor id was unknown at
+ * submission or released in between.  Built on the lazy-factorize, resident-factor semantics of the
  * class (RGF.H:561, 585, 619); the reference has no request loop. */
 enum rgf_request_kind {
   RGF_REQ_FACTOR = 0,   /* create + factorize + logDet; returns factor_id    */

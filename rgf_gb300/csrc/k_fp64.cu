@@ -8,14 +8,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 
 #include "rgf_internal.h"
 
 namespace rgf {
 
 namespace {
-
-constexpr int GBM = 64, GBN = 64, GBK = 16, GPAD = 68;
 
 __device__ __forceinline__ void dmma_8x8x4(double (&c)[2], double a, double b) {
   asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
@@ -27,68 +26,84 @@ struct GemmTileRange {
   int klo, khi;
 };
 
+template <int TM, int TK>
 __device__ __forceinline__ GemmTileRange k_range(const GemmDesc& g, int m0, int n0) {
   int klo = 0, khi = g.k;
-  if (g.triA == TRI_LOWER) khi = min(khi, m0 + GBM);
+  if (g.triA == TRI_LOWER) khi = min(khi, m0 + TM);
   if (g.triA == TRI_UPPER) klo = max(klo, m0);
   if (g.triB == TRI_LOWER) klo = max(klo, n0);
-  if (g.triB == TRI_UPPER) khi = min(khi, n0 + GBN);
-  klo = (klo / GBK) * GBK;
+  if (g.triB == TRI_UPPER) khi = min(khi, n0 + TM);
+  klo = (klo / TK) * TK;
   return {klo, khi};
 }
 
+// TM x TM output tiles, 4 warps of (TM/2) x (TM/2) built from m8n8k4 DMMA
+// fragments, K staged TK at a time.  TM = 64, TK = 16 for large products;
+// TM = 32, TK = 8 spreads small products over four times as many CTAs (each
+// SM retires only ~3.5 FP64 flops per cycle, so a small product on few SMs
+// is slow however short it is).
+template <int TM, int TK>
 __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
-  const int m0 = blockIdx.x * GBM;
-  const int n0 = blockIdx.y * GBN;
-  if (g.outLower && m0 + GBM <= n0) return;  // tile entirely above the diagonal
+  constexpr int F = TM / 16;             // 8 x 8 fragments per warp side
+  constexpr int LPT = TM * TK / 128;     // elements per thread per operand and stage
+  constexpr int PAD = TM + 4;
+  const int m0 = blockIdx.x * TM;
+  const int n0 = blockIdx.y * TM;
+  if (g.outLower && m0 + TM <= n0) return;  // tile entirely above the diagonal
   const bool splitk = g.ksplit > 1;              // blockIdx.z is the K slice, batch == 1
   const long long bz = splitk ? 0 : blockIdx.z;
   const double* __restrict__ A = g.A + bz * g.sA;
+  const double* A2 = g.A2 ? g.A2 + bz * g.sA - g.mA1 : nullptr;
+  const int mA1 = g.A2 ? g.mA1 : g.m;
   const double* __restrict__ B = g.B + bz * g.sB;
   const double* C = g.C ? g.C + bz * g.sC : nullptr;
   double* D = g.D + bz * g.sD;
+  const double* C2 = g.C2 ? g.C2 + bz * g.sC - g.mD1 : nullptr;
+  double* D2 = g.D2 ? g.D2 + bz * g.sD - g.mD1 : nullptr;
+  const int mD1 = g.D2 ? g.mD1 : g.m;
 
-  __shared__ double As[GBK][GPAD];
-  __shared__ double Bs[GBK][GPAD];
+  __shared__ double As[TK][PAD];
+  __shared__ double Bs[TK][PAD];
 
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
-  GemmTileRange kr = k_range(g, m0, n0);
+  const int wm = (warp & 1) * (TM / 2), wn = (warp >> 1) * (TM / 2);
+  GemmTileRange kr = k_range<TM, TK>(g, m0, n0);
   if (splitk) {
     const int len = max(0, kr.khi - kr.klo);
-    const int chunk = ((len + g.ksplit - 1) / g.ksplit + GBK - 1) / GBK * GBK;
+    const int chunk = ((len + g.ksplit - 1) / g.ksplit + TK - 1) / TK * TK;
     const int lo = kr.klo + (int)blockIdx.z * chunk;
     kr.khi = min(kr.khi, lo + chunk);
     kr.klo = lo;
   }
 
-  double acc[4][4][2];
+  double acc[F][F][2];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < F; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+    for (int j = 0; j < F; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
 
-  double ra[8], rb[8];
+  double ra[LPT], rb[LPT];
   auto load = [&](int kt) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < LPT; ++j) {
       int rr, kk;
-      if (!g.transA) { rr = tid & 63; kk = (tid >> 6) + 2 * j; }
-      else           { kk = tid & 15; rr = (tid >> 4) + 8 * j; }
+      if (!g.transA) { rr = tid % TM; kk = tid / TM + (128 / TM) * j; }
+      else           { kk = tid % TK; rr = tid / TK + (128 / TK) * j; }
       const int r = m0 + rr, kg = kt + kk;
       bool ok = r < g.m && kg < kr.khi;
       if (g.triA == TRI_LOWER) ok = ok && kg <= r;
       if (g.triA == TRI_UPPER) ok = ok && kg >= r;
       double v = 0.0;
-      if (ok) v = g.transA ? A[(long long)kg + (long long)r * g.lda] : A[(long long)r + (long long)kg * g.lda];
+      if (ok) v = g.transA ? A[(long long)kg + (long long)r * g.lda]
+                           : (r < mA1 ? A : A2)[(long long)r + (long long)kg * g.lda];
       ra[j] = v;
     }
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < LPT; ++j) {
       int cc, kk;
-      if (!g.transB) { kk = tid & 15; cc = (tid >> 4) + 8 * j; }
-      else           { cc = tid & 63; kk = (tid >> 6) + 2 * j; }
+      if (!g.transB) { kk = tid % TK; cc = tid / TK + (128 / TK) * j; }
+      else           { cc = tid % TM; kk = tid / TM + (128 / TM) * j; }
       const int c = n0 + cc, kg = kt + kk;
       bool ok = c < g.n && kg < kr.khi;
       if (g.triB == TRI_LOWER) ok = ok && kg >= c;
@@ -100,31 +115,31 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
   };
   auto store = [&]() {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      if (!g.transA) As[(tid >> 6) + 2 * j][tid & 63] = ra[j];
-      else           As[tid & 15][(tid >> 4) + 8 * j] = ra[j];
-      if (!g.transB) Bs[tid & 15][(tid >> 4) + 8 * j] = rb[j];
-      else           Bs[(tid >> 6) + 2 * j][tid & 63] = rb[j];
+    for (int j = 0; j < LPT; ++j) {
+      if (!g.transA) As[tid / TM + (128 / TM) * j][tid % TM] = ra[j];
+      else           As[tid % TK][tid / TK + (128 / TK) * j] = ra[j];
+      if (!g.transB) Bs[tid % TK][tid / TK + (128 / TK) * j] = rb[j];
+      else           Bs[tid / TM + (128 / TM) * j][tid % TM] = rb[j];
     }
   };
 
   if (kr.klo < kr.khi) {
     load(kr.klo);
-    for (int kt = kr.klo; kt < kr.khi; kt += GBK) {
+    for (int kt = kr.klo; kt < kr.khi; kt += TK) {
       store();
       __syncthreads();
-      if (kt + GBK < kr.khi) load(kt + GBK);
+      if (kt + TK < kr.khi) load(kt + TK);
 #pragma unroll
-      for (int ks = 0; ks < GBK; ks += 4) {
-        double af[4], bf[4];
+      for (int ks = 0; ks < TK; ks += 4) {
+        double af[F], bf[F];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) af[i] = As[ks + (lane & 3)][wm + i * 8 + (lane >> 2)];
+        for (int i = 0; i < F; ++i) af[i] = As[ks + (lane & 3)][wm + i * 8 + (lane >> 2)];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bf[j] = Bs[ks + (lane & 3)][wn + j * 8 + (lane >> 2)];
+        for (int j = 0; j < F; ++j) bf[j] = Bs[ks + (lane & 3)][wn + j * 8 + (lane >> 2)];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < F; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) dmma_8x8x4(acc[i][j], af[i], bf[j]);
+          for (int j = 0; j < F; ++j) dmma_8x8x4(acc[i][j], af[i], bf[j]);
       }
       __syncthreads();
     }
@@ -133,10 +148,10 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
   if (splitk) {  // raw partial sums of this K slice; reduced in fixed order later
     double* W = g.ws + (long long)blockIdx.z * g.m * g.n;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < F; ++i) {
       const int r = m0 + wm + i * 8 + (lane >> 2);
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int j = 0; j < F; ++j)
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
           const int c = n0 + wn + j * 8 + (lane & 3) * 2 + e;
@@ -146,19 +161,21 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
     return;
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < F; ++i) {
     const int r = m0 + wm + i * 8 + (lane >> 2);
     if (r >= g.m) continue;
+    const double* Cr = r < mD1 ? C : C2;
+    double* Dr = r < mD1 ? D : D2;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < F; ++j) {
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
         const int c = n0 + wn + j * 8 + (lane & 3) * 2 + e;
         if (c >= g.n) continue;
         if (g.outLower && r < c) continue;
         double v = g.alpha * acc[i][j][e];
-        if (g.beta != 0.0) v += g.beta * C[(long long)r + (long long)c * g.ldc];
-        D[(long long)r + (long long)c * g.ldd] = v;
+        if (g.beta != 0.0) v += g.beta * Cr[(long long)r + (long long)c * g.ldc];
+        Dr[(long long)r + (long long)c * g.ldd] = v;
       }
     }
   }
@@ -262,6 +279,103 @@ __global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ld
 }
 
 // ---------------------------------------------------------------------------
+// Leaf Cholesky, data-flow form.  Column c of the tile is owned by warp c % 8
+// (two warps per sub-partition, so all four FP64 units work).  Step j applies
+// column j (final, unscaled, with y_j = S_jj^{-1/2}) to every later column;
+// the owner of column j + 1 updates that column first, takes its pivot from
+// the register that holds the new diagonal and publishes y_{j+1} with a
+// release store, so step j + 1 starts in every warp as soon as its own step-j
+// columns are done and y_{j+1} is visible -- there is no CTA-wide barrier per
+// column.  Columns are written only by their owner; column j is read-only
+// once y_j is published.  Waits are bounded: after ~2^26 polls the kernel
+// records a timeout and every warp leaves the loop.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void st_release_cta(int* p, int v) {
+  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;"
+               :: "r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_cta(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];"
+               : "=r"(v) : "r"((unsigned)__cvta_generic_to_shared(p)) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(256) leaf_potrf_flow_kernel(double* T, long long ldt, int nbk,
+                                                              int col0, double* logpart,
+                                                              DevStatus* st) {
+  __shared__ double S[64][65];
+  __shared__ double ys[64];
+  __shared__ int ready;   // y_0 .. y_ready are published
+  __shared__ int abort_;  // a wait gave up
+  __shared__ int fail;    // smallest non-positive pivot column
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  for (int c = warp; c < nbk; c += 8)
+    for (int r = c + lane; r < nbk; r += 32) S[r][c] = T[(long long)r + (long long)c * ldt];
+  if (tid == 0) {
+    fail = 0x7fffffff;
+    abort_ = 0;
+    ready = -1;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const double d = S[0][0];
+    if (!(d > 0.0)) fail = 0;
+    ys[0] = d > 0.0 ? rsqrt_fast(d) : nan;
+    st_release_cta(&ready, 0);
+  }
+  for (int j = 0; j + 1 < nbk; ++j) {
+    if (ld_acquire_cta(&ready) < j) {
+      int it = 0;
+      while (ld_acquire_cta(&ready) < j && !abort_ && ++it < (1 << 26)) {
+      }
+      if (it >= (1 << 26)) {
+        abort_ = 1;
+        if (lane == 0) atomicExch(&st->timeout, 1);
+      }
+      if (abort_) break;
+    }
+    const double y = ys[j];
+    const double y2 = y * y;
+    int c = j + 1 + ((warp - (j + 1)) % 8 + 8) % 8;  // first owned column > j
+    for (; c < nbk; c += 8) {
+      const double f = S[c][j] * y2;
+      double dnew = 0.0;
+      for (int r = c + lane; r < nbk; r += 32) {
+        const double v = fma(-S[r][j], f, S[r][c]);
+        S[r][c] = v;
+        if (r == c) dnew = v;
+      }
+      if (c == j + 1) {
+        __syncwarp();
+        if (lane == 0) {
+          const bool ok = dnew > 0.0;
+          if (!ok) atomicMin(&fail, c);
+          ys[c] = ok ? rsqrt_fast(dnew) : nan;
+          st_release_cta(&ready, c);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int c = warp; c < nbk; c += 8) {
+    const double y = ys[c];
+    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c] * y;
+  }
+  if (warp == 0) {
+    double v = (lane < nbk ? log(S[lane][lane] * ys[lane]) : 0.0) +
+               (lane + 32 < nbk ? log(S[lane + 32][lane + 32] * ys[lane + 32]) : 0.0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      *logpart = v;
+      if (fail != 0x7fffffff) atomicMin(&st->not_spd_col, col0 + fail);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Row-parallel triangular solve with a <= 64 x 64 lower tile.  On GB300 each
 // SM sub-partition has its own slow FP64 unit (a dependent DFMA takes ~64
 // cycles; one warp reaches a quarter of the SM's FP64 rate), so a CTA is
@@ -270,37 +384,40 @@ __global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ld
 // final.  Loops stay rolled (a fully unrolled solve stalls on instruction
 // fetch).
 // ---------------------------------------------------------------------------
-template <int MODE>
+template <int MODE, int RPB>
 __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs, long long xcs,
                                                          int rows, const double* L, long long ldl,
                                                          int nbk, long long sX, long long sL) {
+  // RPB rows per CTA; the 128 threads are RPB rows x G column groups and
+  // group g applies the updates of the unknowns l = g, g + G, ...
+  constexpr int G = 128 / RPB;
   __shared__ double Ls[64][65];
-  __shared__ double Xs[64][33];
+  __shared__ double Xs[64][RPB + 1];
   __shared__ double rinv[64];
   X += (long long)blockIdx.y * sX;
   L += (long long)blockIdx.y * sL;
-  const int t = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = threadIdx.x % RPB, w = threadIdx.x / RPB;
   for (int idx = threadIdx.x; idx < 64 * 64; idx += 128) {
     const int c = idx >> 6, r = idx & 63;
     double v = 0.0;
     if (r < nbk && c < nbk && r >= c) v = L[(long long)r + (long long)c * ldl];
     Ls[r][c] = v;
   }
-  const long long r = (long long)blockIdx.x * 32 + t;
+  const long long r = (long long)blockIdx.x * RPB + t;
   const bool live = r < rows;
-  for (int j = w; j < nbk; j += 4) Xs[j][t] = live ? X[r * xrs + (long long)j * xcs] : 0.0;
+  for (int j = w; j < nbk; j += G) Xs[j][t] = live ? X[r * xrs + (long long)j * xcs] : 0.0;
   __syncthreads();
   if (threadIdx.x < 64) rinv[threadIdx.x] = (threadIdx.x < nbk) ? 1.0 / Ls[threadIdx.x][threadIdx.x] : 0.0;
   __syncthreads();
   if (MODE == 0) {  // x_j = (b_j - sum_{l<j} x_l L_jl) / L_jj
     for (int j = 0; j < nbk; ++j) {
       const double xj = Xs[j][t] * rinv[j];
-      __syncthreads();  // every warp has read x_j before it is overwritten
+      __syncthreads();  // every group has read x_j before it is overwritten
       if (w == 0) Xs[j][t] = xj;
-      // first unknown > j owned by this warp
-      const int l0 = j + 1 + ((w - (j + 1)) % 4 + 4) % 4;
+      // first unknown > j owned by this group
+      const int l0 = j + 1 + ((w - (j + 1)) % G + G) % G;
 #pragma unroll 4
-      for (int l = l0; l < nbk; l += 4) Xs[l][t] = fma(-xj, Ls[l][j], Xs[l][t]);
+      for (int l = l0; l < nbk; l += G) Xs[l][t] = fma(-xj, Ls[l][j], Xs[l][t]);
       __syncthreads();
     }
   } else {  // x_j = (b_j - sum_{l>j} x_l L_lj) / L_jj, j descending
@@ -309,12 +426,12 @@ __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs
       __syncthreads();
       if (w == 0) Xs[j][t] = xj;
 #pragma unroll 4
-      for (int l = w; l < j; l += 4) Xs[l][t] = fma(-xj, Ls[j][l], Xs[l][t]);
+      for (int l = w; l < j; l += G) Xs[l][t] = fma(-xj, Ls[j][l], Xs[l][t]);
       __syncthreads();
     }
   }
   if (live)
-    for (int j = w; j < nbk; j += 4) X[r * xrs + (long long)j * xcs] = Xs[j][t];
+    for (int j = w; j < nbk; j += G) X[r * xrs + (long long)j * xcs] = Xs[j][t];
 }
 
 // Thin products (m <= 16, op(B) = B^T): lane = output column, the 4 warps of
@@ -359,8 +476,10 @@ __global__ void splitk_reduce_kernel(GemmDesc g) {
   double v = 0.0;
   for (int s = 0; s < g.ksplit; ++s) v += g.ws[s * mn + o];
   v *= g.alpha;
-  if (g.beta != 0.0) v += g.beta * g.C[(long long)r + (long long)c * g.ldc];
-  g.D[(long long)r + (long long)c * g.ldd] = v;
+  const bool hi = g.D2 && r >= g.mD1;
+  const long long ro = hi ? r - g.mD1 : r;
+  if (g.beta != 0.0) v += g.beta * (hi ? g.C2 : g.C)[ro + (long long)c * g.ldc];
+  (hi ? g.D2 : g.D)[ro + (long long)c * g.ldd] = v;
 }
 
 }  // namespace
@@ -370,14 +489,15 @@ double gemm_flops(const GemmDesc& g) {
   double f = 2.0 * m * n * k;
   if (g.triA != TRI_NONE) f = m * (m + 1.0) * n;
   if (g.triB != TRI_NONE) f = m * n * (n + 1.0);
-  if (g.outLower && g.m == g.n && g.n > 0) f = f * (n + 1.0) / (2.0 * n);
+  if (g.outLower && g.m >= g.n && g.n > 0) f = 2.0 * k * (n * (n + 1.0) / 2.0 + (m - n) * n);
   return f * g.batch;
 }
 
 int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
   if (g0.m <= 0 || g0.n <= 0 || g0.batch <= 0) return 0;
   GemmDesc g = g0;
-  if (g.m <= 16 && g.transB && g.triA == TRI_NONE && g.batch == 1 && g.ws && !g.outLower) {
+  if (g.m <= 16 && g.transB && g.triA == TRI_NONE && g.batch == 1 && g.ws && !g.outLower &&
+      !g.A2) {
     const int cx = (g.n + 31) / 32;
     int kchunks = std::max(1, std::min((2 * 152 + cx - 1) / cx, (g.k + 63) / 64));
     while (kchunks > 1 && (long long)kchunks * g.m * g.n > g.ws_elems) --kchunks;
@@ -390,24 +510,34 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
       return 2;
     }
   }
-  const int tx = (g.m + GBM - 1) / GBM, ty = (g.n + GBN - 1) / GBN;
-  // too few output tiles for 152 SMs (each SM retires only ~3.5 FP64 flops
-  // per cycle, so one 64x64x64 tile is tens of microseconds): split K
-  int ksplit = 1;
-  if (g.batch == 1 && g.ws && g.k >= 32) {
+  // tiles of 64 when they (with split K) cover the SMs, else tiles of 32
+  auto count_tiles = [&](int tm) {
+    const int tx = (g.m + tm - 1) / tm, ty = (g.n + tm - 1) / tm;
     long long tiles = 0;
     for (int bx = 0; bx < tx; ++bx)
       for (int by = 0; by < ty; ++by)
-        if (!(g.outLower && bx * GBM + GBM <= by * GBN)) ++tiles;
+        if (!(g.outLower && bx * tm + tm <= by * tm)) ++tiles;
+    return tiles;
+  };
+  const long long t64 = count_tiles(64);
+  const bool small = g.batch == 1 && g.ws && t64 * std::min(16, std::max(1, g.k / 16)) < 152;
+  const int tm = small ? 32 : 64, tk = small ? 8 : 16;
+  const long long tiles = small ? count_tiles(32) : t64;
+  // too few output tiles for 152 SMs (each SM retires only ~3.5 FP64 flops
+  // per cycle, so one 64x64x64 tile is tens of microseconds): split K
+  int ksplit = 1;
+  if (g.batch == 1 && g.ws && g.k >= 2 * tk) {
     if (tiles > 0 && tiles < 2 * 152) {
       ksplit = (int)std::min<long long>(16, (3 * 152 + tiles - 1) / tiles);
-      ksplit = std::min(ksplit, g.k / 16);
+      ksplit = std::min(ksplit, g.k / tk);
       while (ksplit > 1 && (long long)ksplit * g.m * g.n > g.ws_elems) --ksplit;
     }
   }
   g.ksplit = ksplit;
+  const int tx = (g.m + tm - 1) / tm, ty = (g.n + tm - 1) / tm;
   dim3 grid(tx, ty, ksplit > 1 ? ksplit : g.batch);
-  gemm_fp64_kernel<<<grid, 128, 0, s>>>(g);
+  if (small) gemm_fp64_kernel<32, 8><<<grid, 128, 0, s>>>(g);
+  else gemm_fp64_kernel<64, 16><<<grid, 128, 0, s>>>(g);
   if (ksplit > 1) {
     dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
     splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
@@ -419,18 +549,38 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, double* logpart,
                        DevStatus* st, cudaStream_t s) {
   if (nbk <= 0) return;
-  leaf_potrf_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, logpart, st);
+  static const int variant = [] {
+    const char* e = getenv("RGF_GB300_LEAF_KERNEL");
+    return e ? atoi(e) : 1;
+  }();
+  if (variant == 1)
+    leaf_potrf_flow_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, logpart, st);
+  else
+    leaf_potrf_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, logpart, st);
 }
 
 void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,
                       long long ldl, int nbk, int mode, int batch, long long sX, long long sL,
                       cudaStream_t s) {
   if (rows <= 0 || nbk <= 0 || batch <= 0) return;
-  dim3 grid((rows + 31) / 32, batch);
-  if (mode == 0)
-    trsm_rows_kernel<0><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
-  else
-    trsm_rows_kernel<1><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+  // Each SM retires only ~3.5 FP64 flops per cycle, so a solve spread over
+  // fewer CTAs than SMs is slow: take fewer rows per CTA when the grid is small.
+  const long long ctas32 = (long long)((rows + 31) / 32) * batch;
+  const int rpb = ctas32 >= 2 * 152 ? 32 : ctas32 * 2 >= 152 ? 16 : 8;
+  dim3 grid((rows + rpb - 1) / rpb, batch);
+#define RGF_TRSM_LAUNCH(R)                                                                   \
+  if (mode == 0)                                                                            \
+    trsm_rows_kernel<0, R><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);    \
+  else                                                                                      \
+    trsm_rows_kernel<1, R><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+  if (rpb == 32) {
+    RGF_TRSM_LAUNCH(32)
+  } else if (rpb == 16) {
+    RGF_TRSM_LAUNCH(16)
+  } else {
+    RGF_TRSM_LAUNCH(8)
+  }
+#undef RGF_TRSM_LAUNCH
 }
 
 }  // namespace rgf

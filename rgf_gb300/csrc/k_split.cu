@@ -6,11 +6,13 @@
 //     c of op(B) likewise with 2^-eb[c].  The cut is done on the FP64 bit
 //     pattern with integer instructions only (no FP64 arithmetic).
 //  2. for every digit pair (s, t) with s + t <= S + 1 the tensor cores form
-//     the integer products P_st = A_s B_t, 1024 terms at a time, in FP32 in
-//     tensor memory; with beta = 7 each 1024-term sum is below 2^24 and thus
-//     exact.
+//     the integer products P_st = A_s B_t in FP32 in tensor memory.  Pairs of
+//     one level (s + t) share an accumulator; a job sums the level's pairs over
+//     a K range of at most 1024 terms in total, so with beta = 7 every sum is
+//     below 2^24 and thus exact;
 //  3. each exact partial is moved to registers and added, shifted by its
-//     level, into a 64-bit integer fixed-point accumulator;
+//     level, into a 64-bit integer fixed-point accumulator (integer sums: the
+//     result does not depend on how terms are grouped into jobs);
 //  4. one conversion to FP64 per output, scaled by 2^(ea[r] + eb[c] + ...).
 // The GEMM kernel is warp specialized: one warp issues TMA tile loads
 // (cp.async.bulk.tensor, 128B swizzle) into a 4-stage shared-memory ring, one
@@ -36,7 +38,10 @@ namespace rgf {
 namespace {
 
 constexpr int BM = 128, BN = 128, BKE = 64;  // tile rows, cols, K elements per stage
-constexpr int NSTAGE = 4;
+#ifndef RGF_SPLIT_NSTAGE
+#define RGF_SPLIT_NSTAGE 4
+#endif
+constexpr int NSTAGE = RGF_SPLIT_NSTAGE;
 constexpr int KCHUNK_BLOCKS = 16;             // 16 x 64 = 1024 terms per exact FP32 sum
 constexpr int SPLIT_BETA = 7;
 constexpr int MAXPAIRS = 45;
@@ -57,6 +62,9 @@ struct SplitParams {
   long long ldc, sC;
   double* D;
   long long ldd, sD;
+  const double* C2;  // rows >= mD1 of C and D (at C2/D2 + r - mD1), or nullptr
+  double* D2;
+  int mD1;
   double alpha, betac;
   DevStatus* st;
 };
@@ -189,6 +197,10 @@ __device__ __forceinline__ void tile_kblocks(const SplitParams& p, int m0, int n
   kb_hi = hi > lo ? (hi + BKE - 1) / BKE : kb_lo;
 }
 
+// K blocks per job at level l (l + 1 pairs share the accumulator): at most
+// 1024 product terms per exact FP32 sum.
+__device__ __forceinline__ int level_chunk(int l) { return max(1, KCHUNK_BLOCKS / (l + 1)); }
+
 // ---- the slice-product GEMM ---------------------------------------------------
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
@@ -214,8 +226,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   int kb_lo, kb_hi;
   tile_kblocks(p, m0, n0, kb_lo, kb_hi);
   const int nkb = kb_hi - kb_lo;
-  const int nchunks = (nkb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
-  const int njobs = nchunks * p.npairs;
+  // jobs: for each level l (pairs l*(l+1)/2 .. +l), K chunks of
+  // KCHUNK_BLOCKS / (l + 1) blocks (1024 terms over the level's pairs)
+  int njobs = 0;
+  for (int l = 0; l < p.S; ++l) njobs += nkb > 0 ? (nkb + level_chunk(l) - 1) / level_chunk(l) : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
@@ -244,16 +258,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       long long use = 0;
-      for (int j = 0; j < njobs && !*abort_flag; ++j) {
-        const int c = j / p.npairs, pr = j % p.npairs;
-        const int kb0 = kb_lo + c * KCHUNK_BLOCKS, kb1 = min(kb_hi, kb0 + KCHUNK_BLOCKS);
-        for (int kb = kb0; kb < kb1; ++kb, ++use) {
-          const int s = (int)(use % NSTAGE);
-          const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
-          if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, p.st)) break;
-          mbar_expect_tx(&full[s], 2 * TILE_BYTES);
-          tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], kb * BKE, m0, zS + p.ps[pr]);
-          tma_load_3d(tilesB + s * TILE_BYTES, &tmB, &full[s], kb * BKE, n0, zS + p.pt[pr]);
+      bool ok = true;
+      for (int l = 0; l < p.S && ok; ++l) {
+        const int chunk = level_chunk(l), p0 = l * (l + 1) / 2;
+        for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk) {
+          const int kb1 = min(kb_hi, kb0 + chunk);
+          for (int pr = p0; pr <= p0 + l && ok; ++pr)
+            for (int kb = kb0; kb < kb1; ++kb, ++use) {
+              const int s = (int)(use % NSTAGE);
+              const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
+              if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, p.st)) { ok = false; break; }
+              mbar_expect_tx(&full[s], 2 * TILE_BYTES);
+              tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], kb * BKE, m0, zS + p.ps[pr]);
+              tma_load_3d(tilesB + s * TILE_BYTES, &tmB, &full[s], kb * BKE, n0, zS + p.pt[pr]);
+            }
         }
       }
       // let in-flight loads land before the CTA can exit
@@ -266,30 +284,36 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       long long use = 0;
-      for (int j = 0; j < njobs && !*abort_flag; ++j) {
-        const int buf = j & 1;
-        const uint32_t aph = (uint32_t)((j >> 1) & 1);
-        if (!mbar_wait(&acc_empty[buf], aph ^ 1u, abort_flag, p.st)) break;
-        tc_fence_after();
-        const uint32_t tacc = tmem_base + (uint32_t)(buf * BN);
-        const int c = j / p.npairs;
-        const int kb0 = kb_lo + c * KCHUNK_BLOCKS, kb1 = min(kb_hi, kb0 + KCHUNK_BLOCKS);
-        bool ok = true;
-        for (int kb = kb0; kb < kb1; ++kb, ++use) {
-          const int s = (int)(use % NSTAGE);
-          const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
-          if (!mbar_wait(&full[s], ph, abort_flag, p.st)) { ok = false; break; }
+      int j = 0;
+      bool ok = true;
+      for (int l = 0; l < p.S && ok; ++l) {
+        const int chunk = level_chunk(l);
+        for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk, ++j) {
+          const int kb1 = min(kb_hi, kb0 + chunk);
+          const int buf = j & 1;
+          const uint32_t aph = (uint32_t)((j >> 1) & 1);
+          if (!mbar_wait(&acc_empty[buf], aph ^ 1u, abort_flag, p.st)) { ok = false; break; }
           tc_fence_after();
-          const uint64_t ad = smem_desc_sw128(tilesA + s * TILE_BYTES);
-          const uint64_t bd = smem_desc_sw128(tilesB + s * TILE_BYTES);
+          const uint32_t tacc = tmem_base + (uint32_t)(buf * BN);
+          bool first = true;
+          for (int pr = 0; pr <= l && ok; ++pr)
+            for (int kb = kb0; kb < kb1; ++kb, ++use) {
+              const int s = (int)(use % NSTAGE);
+              const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
+              if (!mbar_wait(&full[s], ph, abort_flag, p.st)) { ok = false; break; }
+              tc_fence_after();
+              const uint64_t ad = smem_desc_sw128(tilesA + s * TILE_BYTES);
+              const uint64_t bd = smem_desc_sw128(tilesB + s * TILE_BYTES);
 #pragma unroll
-          for (int kk = 0; kk < BKE / 16; ++kk)  // +32 bytes per K=16 step inside the swizzle atom
-            umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2),
-                      (kb > kb0 || kk > 0) ? 1u : 0u);
-          umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+              for (int kk = 0; kk < BKE / 16; ++kk) {  // +32 bytes per K=16 step in the swizzle atom
+                umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2), first ? 0u : 1u);
+                first = false;
+              }
+              umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+            }
+          if (!ok) break;
+          umma_commit(&acc_full[buf]);  // accumulator ready for the drain warps
         }
-        if (!ok) break;
-        umma_commit(&acc_full[buf]);  // accumulator ready for the drain warps
       }
       // wait for the last commit so no MMA is in flight at exit
       if (njobs > 0 && !*abort_flag) {
@@ -305,13 +329,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     long long acc[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) acc[i] = 0;
-    for (int j = 0; j < njobs; ++j) {
+    int l = 0, jl = 0;  // level of job j and job index within the level
+    const int nch0 = nkb > 0 ? (nkb + level_chunk(0) - 1) / level_chunk(0) : 0;
+    int nch = nch0;
+    for (int j = 0; j < njobs; ++j, ++jl) {
+      while (jl >= nch) {
+        ++l;
+        jl = 0;
+        nch = (nkb + level_chunk(l) - 1) / level_chunk(l);
+      }
       const int buf = j & 1;
       if (!mbar_wait(&acc_full[buf], (uint32_t)((j >> 1) & 1), abort_flag, p.st)) break;
       tc_fence_after();
-      const int pr = j % p.npairs;
-      const int level = p.ps[pr] + p.pt[pr] + 2;
-      const int sh = p.beta * (p.S + 1 - level) - p.cs;
+      const int sh = p.beta * (p.S - 1 - l) - p.cs;
       const uint32_t taddr =
           tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + half * 64);
 #pragma unroll
@@ -332,8 +362,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int r = m0 + row;
     if (r < p.m && !*abort_flag) {
       const int* exB = p.exB + (long long)zb * p.exB_stride;
-      const double* C = p.C ? p.C + (long long)zb * p.sC : nullptr;
-      double* D = p.D + (long long)zb * p.sD;
+      const bool hi = p.D2 && r >= p.mD1;
+      const double* C = hi ? p.C2 + (long long)zb * p.sC - p.mD1
+                           : (p.C ? p.C + (long long)zb * p.sC : nullptr);
+      double* D = hi ? p.D2 + (long long)zb * p.sD - p.mD1 : p.D + (long long)zb * p.sD;
       const int er = p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1);
       const int cbase = n0 + half * 64;
 #pragma unroll
@@ -371,11 +403,13 @@ __device__ __forceinline__ int exp_of_max(unsigned long long mx) {
 
 // rows contiguous (rs == 1): thread per row, blockIdx.y picks a 32-term
 // slice of K, partial maxima of |x| (as bit patterns) meet in atomicMax.
+// Rows >= R1 are read from X2 (row r at X2 + (r - R1)) when X2 is set.
 __global__ void rowmax_rowmajor_kernel(const double* X, long long ks, int R, int K, int tri,
-                                       unsigned long long* mx, long long sX, int Rp) {
+                                       unsigned long long* mx, long long sX, int Rp,
+                                       const double* X2, int R1) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
-  X += (long long)blockIdx.z * sX;
+  X = (X2 && r >= R1 ? X2 - R1 : X) + (long long)blockIdx.z * sX;
   mx += (long long)blockIdx.z * Rp;
   const int k0 = blockIdx.y * 32, k1 = min(K, k0 + 32);
   unsigned long long m = 0;
@@ -420,11 +454,13 @@ __global__ void row_exp_kernel(const unsigned long long* mx, int* ex, int Rp) {
 
 // 32 x 32 tiles through shared memory: read coalesced along the contiguous
 // dimension, write the S digit planes coalesced along k.
+// With X2 set (rs == 1 only), rows >= R1 are read from X2 + (r - R1).
 __global__ void slice_kernel(const double* X, long long rs, long long ks, int R, int K, int tri,
                              const int* ex, __nv_bfloat16* out, int Rp, int Kp, int S, int beta,
-                             long long sX) {
+                             long long sX, const double* X2, int R1) {
   __shared__ double tile[32][33];
   X += (long long)blockIdx.z * sX;
+  const double* Xb = X2 ? X2 - R1 + (long long)blockIdx.z * sX : X;
   ex += (long long)blockIdx.z * Rp;
   out += (size_t)blockIdx.z * S * Rp * Kp;
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
@@ -436,7 +472,8 @@ __global__ void slice_kernel(const double* X, long long rs, long long ks, int R,
     else         { kl = tx; rl = ty + 8 * i; }
     const int r = r0 + rl, k = k0 + kl;
     double v = 0.0;
-    if (r < R && k < K && tri_ok(tri, r, k)) v = X[(long long)r * rs + (long long)k * ks];
+    if (r < R && k < K && tri_ok(tri, r, k))
+      v = (X2 && r >= R1 ? Xb : X)[(long long)r * rs + (long long)k * ks];
     tile[rl][kl] = v;
   }
   __syncthreads();
@@ -463,6 +500,114 @@ __global__ void slice_kernel(const double* X, long long rs, long long ks, int R,
       const int d = (int)((xi >> (beta * (S - 1 - s))) & dmask);
       o[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
     }
+  }
+}
+
+// Both operands of a product with a short K in one launch: a CTA owns 32 rows
+// of op(A) or op(B) (blockIdx.x below nblkA: A), finds their maximum
+// magnitudes over all of K, then writes the S digit planes tile by tile.
+// Replaces the max / exponent / slice kernels (and the memsets) of the long-K
+// path, which dominate small products.
+struct SliceOperand {
+  const double* X;
+  const double* X2;  // rows >= R1 from X2 + (r - R1) (rs == 1 only), or nullptr
+  long long rs, ks, sX;
+  int R, R1, Rp, tri;
+  int* ex;
+  __nv_bfloat16* out;
+};
+
+__global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOperand b, int nblkA,
+                                                          int K, int Kp, int S, int beta) {
+  __shared__ double tile[32][33];
+  __shared__ unsigned long long red[8][33];
+  const bool isA = (int)blockIdx.x < nblkA;
+  const SliceOperand& o = isA ? a : b;
+  const int r0 = (isA ? blockIdx.x : blockIdx.x - nblkA) * 32;
+  const long long z = blockIdx.z;
+  const double* X = o.X + z * o.sX;
+  const double* Xb = o.X2 ? o.X2 - o.R1 + z * o.sX : X;
+  int* ex = o.ex + z * o.Rp;
+  __nv_bfloat16* out = o.out + (size_t)z * S * o.Rp * Kp;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  auto val = [&](int r, int k) -> double {
+    if (r >= o.R || k >= K || !tri_ok(o.tri, r, k)) return 0.0;
+    return (o.X2 && r >= o.R1 ? Xb : X)[(long long)r * o.rs + (long long)k * o.ks];
+  };
+  // pass 1: row maxima of |x| as bit patterns
+  if (o.rs == 1) {  // rows contiguous: lane = row, warp = k phase
+    unsigned long long m = 0;
+    for (int k = ty; k < K; k += 8) {
+      const unsigned long long v =
+          (unsigned long long)__double_as_longlong(val(r0 + tx, k)) & 0x7fffffffffffffffull;
+      m = v > m ? v : m;
+    }
+    red[ty][tx] = m;
+  } else {  // k contiguous: warp = 4 rows, lane = k phase
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int rl = ty + 8 * i;
+      unsigned long long m = 0;
+      for (int k = tx; k < K; k += 32) {
+        const unsigned long long v =
+            (unsigned long long)__double_as_longlong(val(r0 + rl, k)) & 0x7fffffffffffffffull;
+        m = v > m ? v : m;
+      }
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, d);
+        m = y > m ? y : m;
+      }
+      if (tx == 0) red[0][rl] = m;
+    }
+  }
+  __syncthreads();
+  __shared__ int exs[32];
+  if (threadIdx.x < 32) {
+    unsigned long long m = red[0][threadIdx.x];
+    if (o.rs == 1)
+      for (int w = 1; w < 8; ++w) m = red[w][threadIdx.x] > m ? red[w][threadIdx.x] : m;
+    const int r = r0 + threadIdx.x;
+    const int e = r < o.R ? exp_of_max(m) : 0;
+    exs[threadIdx.x] = e;
+    if (r < o.Rp) ex[r] = e;
+  }
+  __syncthreads();
+  // pass 2: digits, one 32 x 32 tile at a time (read along the contiguous
+  // dimension, write along k)
+  const unsigned long long dmask = (1ull << beta) - 1ull;
+  const size_t plane = (size_t)o.Rp * Kp;
+  for (int k0 = 0; k0 < Kp; k0 += 32) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int rl, kl;
+      if (o.rs == 1) { rl = tx; kl = ty + 8 * i; }
+      else           { kl = tx; rl = ty + 8 * i; }
+      tile[rl][kl] = val(r0 + rl, k0 + kl);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int rl = ty + 8 * i, r = r0 + rl, k = k0 + tx;
+      if (r >= o.Rp) continue;
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(tile[rl][tx]);
+      const bool neg = (bits >> 63) != 0;
+      int E = (int)((bits >> 52) & 0x7ff);
+      unsigned long long mant = bits & 0xfffffffffffffull;
+      if (E) mant |= 1ull << 52; else E = 1;
+      const int sh = (E - 1075) + beta * S - exs[rl];
+      unsigned long long xi = 0;
+      if (mant != 0) {
+        if (sh >= 0) xi = sh < 64 ? (mant << sh) : 0ull;
+        else xi = -sh < 64 ? (mant >> (-sh)) : 0ull;
+      }
+      __nv_bfloat16* q = out + (size_t)r * Kp + k;
+      for (int s = 0; s < S; ++s) {
+        const int d = (int)((xi >> (beta * (S - 1 - s))) & dmask);
+        q[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -541,6 +686,7 @@ int SplitEngine::ensure_ws(size_t bytes) {
 
 namespace {
 constexpr int MAX_SLICES = 8;
+constexpr int SHORT_K = 512;  // products with K up to this slice both operands in one launch
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // bytes of workspace one batch item of an (RpA x Kp) by (RpB x Kp) problem needs
 size_t item_bytes(int S, int RpA, int RpB, int Kp) {
@@ -578,8 +724,10 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
   const int S = slices > 0 ? std::min(slices, MAX_SLICES) : slices_, beta = SPLIT_BETA;
   const int Kp = round_up(g.k, BKE);
   const int RpA = round_up(g.m, BM), RpB = round_up(g.n, BM);
+  // op(B)^T is op(A) or its first n rows: the slices (and exponents) of A serve both
   const bool same = g.A == g.B && g.lda == g.ldb && g.sA == g.sB && g.transA != g.transB &&
-                    g.m == g.n && g.triA == TRI_NONE && g.triB == TRI_NONE;
+                    g.n <= g.m && (!g.A2 || g.n <= g.mA1) && g.triA == TRI_NONE &&
+                    g.triB == TRI_NONE;
   const size_t per_item = item_bytes(S, RpA, same ? 0 : RpB, Kp);
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>(g.batch, ws_bytes_ / per_item));
   // the split itself: pairs (s, t) with s + t <= S + 1, ordered by level
@@ -623,11 +771,12 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
     unsigned long long* mxB = reinterpret_cast<unsigned long long*>(q);
     // rows of op(X): (r, k) at X[r*rs + k*ks]; digits into out, exponents into ex
     auto slice = [&](const double* X, long long rs, long long ks, long long sX, int R, int tri,
-                     int* ex, unsigned long long* mx, __nv_bfloat16* out, int Rp) {
+                     int* ex, unsigned long long* mx, __nv_bfloat16* out, int Rp,
+                     const double* X2 = nullptr, int R1 = 0) {
       if (rs == 1) {
         cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rp * nbat, s);
         dim3 grid((R + 127) / 128, (g.k + 31) / 32, nbat);
-        rowmax_rowmajor_kernel<<<grid, 128, 0, s>>>(X, ks, R, g.k, tri, mx, sX, Rp);
+        rowmax_rowmajor_kernel<<<grid, 128, 0, s>>>(X, ks, R, g.k, tri, mx, sX, Rp, X2, R1);
       } else {
         dim3 grid((Rp * 32 + 255) / 256, nbat);
         rowmax_kmajor_kernel<<<grid, 256, 0, s>>>(X, rs, R, g.k, tri, mx, Rp, sX);
@@ -635,16 +784,28 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       row_exp_kernel<<<dim3((Rp + 255) / 256, nbat), 256, 0, s>>>(mx, ex, Rp);
       dim3 grid(Kp / 32, Rp / 32, nbat);
       slice_kernel<<<grid, dim3(32, 8), 0, s>>>(X, rs, ks, R, g.k, tri, ex, out, Rp, Kp, S, beta,
-                                                sX);
+                                                sX, X2, R1);
       launched += 3;
     };
     const double* A = g.A + (long long)b0 * g.sA;
-    if (!g.transA) slice(A, 1, g.lda, g.sA, g.m, g.triA, exA, mxA, sa, RpA);
-    else slice(A, g.lda, 1, g.sA, g.m, g.triA, exA, mxA, sa, RpA);
-    if (!same) {
-      const double* B = g.B + (long long)b0 * g.sB;
-      if (!g.transB) slice(B, g.ldb, 1, g.sB, g.n, triBt, exB, mxB, sb, RpB);
-      else slice(B, 1, g.ldb, g.sB, g.n, triBt, exB, mxB, sb, RpB);
+    const double* A2 = g.A2 ? g.A2 + (long long)b0 * g.sA : nullptr;
+    const double* B = g.B + (long long)b0 * g.sB;
+    if (Kp <= SHORT_K) {
+      SliceOperand oa{A, A2, g.transA ? g.lda : 1, g.transA ? 1 : g.lda, g.sA, g.m,
+                      A2 ? g.mA1 : g.m, RpA, g.triA, exA, sa};
+      SliceOperand ob{B, nullptr, g.transB ? 1 : g.ldb, g.transB ? g.ldb : 1, g.sB, g.n, g.n,
+                      RpB, triBt, exB, sb};
+      const int nblkA = RpA / 32, nblkB = same ? 0 : RpB / 32;
+      slice_pair_kernel<<<dim3(nblkA + nblkB, 1, nbat), 256, 0, s>>>(oa, ob, nblkA, g.k, Kp, S,
+                                                                     beta);
+      launched += 1;
+    } else {
+      if (!g.transA) slice(A, 1, g.lda, g.sA, g.m, g.triA, exA, mxA, sa, RpA, A2, g.mA1);
+      else slice(A, g.lda, 1, g.sA, g.m, g.triA, exA, mxA, sa, RpA);
+      if (!same) {
+        if (!g.transB) slice(B, g.ldb, 1, g.sB, g.n, triBt, exB, mxB, sb, RpB);
+        else slice(B, 1, g.ldb, g.sB, g.n, triBt, exB, mxB, sb, RpB);
+      }
     }
     CUtensorMap ma, mb;
     if (!make_map(&ma, sa, S * nbat, RpA, Kp) ||
@@ -652,6 +813,9 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       GemmDesc f = g;  // cannot describe the operands: FP64 kernel for this chunk
       f.batch = nbat;
       f.A = A; f.B = g.B + (long long)b0 * g.sB;
+      if (g.A2) f.A2 = g.A2 + (long long)b0 * g.sA;
+      if (g.C2) f.C2 = g.C2 + (long long)b0 * g.sC;
+      if (g.D2) f.D2 = g.D2 + (long long)b0 * g.sD;
       f.C = g.C ? g.C + (long long)b0 * g.sC : nullptr;
       f.D = g.D + (long long)b0 * g.sD;
       launched += launch_gemm_fp64(f, s);
@@ -660,6 +824,9 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
     p.exA = exA; p.exB = exB;
     p.C = g.C ? g.C + (long long)b0 * g.sC : nullptr;
     p.D = g.D + (long long)b0 * g.sD;
+    p.C2 = g.C2 ? g.C2 + (long long)b0 * g.sC : nullptr;
+    p.D2 = g.D2 ? g.D2 + (long long)b0 * g.sD : nullptr;
+    p.mD1 = g.mD1;
     dim3 grid(RpA / BM, RpB / BN, nbat);
     if (tensor_flops) {
       double tiles = 0.0;  // lower-only outputs skip tiles above the diagonal

@@ -32,6 +32,12 @@ constexpr int NB = 64;  // leaf tile of the FP64 panel Cholesky / triangular sol
 struct rgf_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // Second stream of the panel factorization: the rows below a diagonal block
+  // (off the column-to-column critical path) are solved and updated there.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool on_side = false;  // launch wrappers issue to `side`
+  bool lookahead = true;
   BtaShape sh{};
   long long nnz = 0, mf_size = 0;
   rgf_opts opts{};
@@ -42,7 +48,7 @@ struct rgf_handle {
   double* d_MF = nullptr;
   double* d_MS = nullptr;
   double* d_U = nullptr;     // Linv^T of every diagonal block (ns x ns each), then the corner
-  double* d_T1 = nullptr;    // ns x ns
+  double* d_T1 = nullptr;    // (ns + nd) x ns
   double* d_T2 = nullptr;    // ns x ns
   double* d_T3 = nullptr;    // nd x ns
   double* d_logpart = nullptr;
@@ -56,6 +62,7 @@ struct rgf_handle {
   size_t partial_cap = 0;
   double* d_res = nullptr;      // residual scratch: x, b, y (3n)
   double* d_gemm_ws = nullptr;  // split-K partial sums of small FP64 GEMMs
+  double* d_gemm_ws_side = nullptr;  // the same for the side stream
   long long gemm_ws_elems = 0;
 
   bool factored = false;
@@ -70,7 +77,8 @@ struct rgf_handle {
   long long kernels_total = 0;    // kernels launched over the handle's life
 
   SplitEngine* split = nullptr;
-  int nb = 64;  // leaf width of the panel Cholesky (<= 64)
+  SplitEngine* split_side = nullptr;  // own slice workspace for the side stream
+  int nb = 32;  // leaf width of the panel Cholesky (<= 64)
 
   // kernel timer: per class (1 = FP64 DMMA GEMM, 2 = split tensor-core GEMM)
   struct TimedLaunch {
@@ -134,6 +142,20 @@ void dfree(void* p) {
 // only when the handle does not keep diagonal blocks in FP64.
 enum GemmClass { SMALL = 0, BULK = 1, DIAG = 2 };
 
+cudaStream_t cur_stream(const rgf_handle* h) { return h->on_side ? h->side : h->stream; }
+
+// Work issued to the side stream after fork_side waits for everything issued
+// to the main stream before it; join_side makes the main stream wait for the
+// side stream.  Both are plain event dependencies (graph edges when captured).
+void fork_side(rgf_handle* h) {
+  cudaEventRecord(h->ev_fork, h->stream);
+  cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+}
+void join_side(rgf_handle* h) {
+  cudaEventRecord(h->ev_join, h->side);
+  cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+}
+
 void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
   const bool bulk = cls != SMALL;
@@ -152,43 +174,45 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
       e1 = h->ev_pool.back().second;
       h->ev_pool.pop_back();
     }
-    cudaEventRecord(e0, h->stream);
+    cudaEventRecord(e0, cur_stream(h));
   }
   long long launched = 1;
   double tflops = 0.0;
-  bool split = h->split && may_split && h->split->supports(g);
+  SplitEngine* eng = h->on_side ? h->split_side : h->split;
+  bool split = eng && may_split && eng->supports(g);
   if (split) {
     // Route by estimated time.  A split product has a fixed cost of a few
     // small slicing kernels and tensor tiles padded to 128 x 128; the FP64
     // DMMA kernel (split-K for small grids) has almost none but runs at
     // ~1 TFLOP/s.  Small or thin products are faster in FP64 (which is also
     // FP64-accurate).
-    const int S = slices > 0 ? slices : h->split->slices();
+    const int S = slices > 0 ? slices : eng->slices();
     const double pairs = S * (S + 1) / 2.0;
     auto up = [](double x, double m) { return std::ceil(x / m) * m; };
-    const double t_split = (g.A == g.B ? 40e-6 : 70e-6) +
-                           pairs * 2.0 * up(g.m, 128) * up(g.n, 128) * up(g.k, 64) * g.batch /
-                               700e12;
+    // short K: both operands sliced in one launch
+    const double fixed = up(g.k, 64) <= 512 ? 15e-6 : (g.A == g.B ? 40e-6 : 70e-6);
+    const double t_split = fixed + pairs * 2.0 * up(g.m, 128) * up(g.n, 128) * up(g.k, 64) *
+                                       g.batch / 700e12;
     const double t_fp64 = 8e-6 + gemm_flops(g) / 0.8e12;
     split = t_split < t_fp64;
   }
   if (split) {
-    launched = h->split->gemm(g, h->stream, h->d_status, &tflops, slices);
+    launched = eng->gemm(g, cur_stream(h), h->d_status, &tflops, slices);
   } else {
     GemmDesc gw = g;
-    gw.ws = h->d_gemm_ws;
+    gw.ws = h->on_side ? h->d_gemm_ws_side : h->d_gemm_ws;
     gw.ws_elems = h->gemm_ws_elems;
-    launched = launch_gemm_fp64(gw, h->stream);
+    launched = launch_gemm_fp64(gw, cur_stream(h));
   }
   h->kernels_issued += launched;
   if (e0) {
-    cudaEventRecord(e1, h->stream);
+    cudaEventRecord(e1, cur_stream(h));
     h->ev_used.push_back({e0, e1, split ? 2 : 1, gemm_flops(g), tflops, g.m, g.n, g.k, g.batch, cls});
   }
 }
 
 void leaf_potrf(rgf_handle* h, double* T, long long ldt, int nbk, int col0, double* part) {
-  launch_leaf_potrf(T, ldt, nbk, col0, part, h->d_status, h->stream);
+  launch_leaf_potrf(T, ldt, nbk, col0, part, h->d_status, cur_stream(h));
   h->kernels_issued++;
 }
 
@@ -196,7 +220,7 @@ void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
                const double* L, long long ldl, int nbk, int mode, int batch = 1,
                long long sX = 0, long long sL = 0) {
   if (rows <= 0) return;
-  launch_trsm_rows(X, xrs, xcs, rows, L, ldl, nbk, mode, batch, sX, sL, h->stream);
+  launch_trsm_rows(X, xrs, xcs, rows, L, ldl, nbk, mode, batch, sX, sL, cur_stream(h));
   h->kernels_issued++;
 }
 
@@ -207,18 +231,33 @@ void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
 // with an inner dimension of half the range, so most of the work runs in a
 // few large products; 64-column leaves are factored in FP64 in one CTA and
 // solved against row-parallel.
-void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int col0,
+//
+// Rows [0, dr) belong to the diagonal block being factored (the column-to-
+// column critical path); rows [dr, rows) are the block rows below it, which
+// nothing on that path reads.  With look-ahead on, their solves and updates
+// go to the side stream, ordered after the main-stream work they read, so the
+// critical path only carries the diagonal block.
+void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int dr, int col0,
                  int part0) {
   const int nb = h->nb;
+  const bool la = h->lookahead && h->side;
+  const int split_row = la ? dr : rows;  // rows at or past this go to the side stream
   if (cols <= nb) {
     leaf_potrf(h, P, lda, cols, col0, h->d_logpart + part0);
-    if (rows > cols) trsm_rows(h, P + cols, 1, lda, rows - cols, P, lda, cols, 0);
+    if (split_row > cols) trsm_rows(h, P + cols, 1, lda, split_row - cols, P, lda, cols, 0);
+    if (rows > split_row) {
+      fork_side(h);
+      h->on_side = true;
+      trsm_rows(h, P + split_row, 1, lda, rows - split_row, P, lda, cols, 0);
+      h->on_side = false;
+    }
     return;
   }
   const int c1 = ((cols / 2 + nb - 1) / nb) * nb;
-  panel_potrf(h, P, lda, rows, c1, col0, part0);
+  panel_potrf(h, P, lda, rows, c1, dr, col0, part0);
   // trailing update: P[c1:rows, c1:cols] -= P[c1:rows, 0:c1] P[c1:cols, 0:c1]^T
   auto upd = [&](int r0, int m, int cls) {
+    if (m <= 0) return;
     GemmDesc g;
     g.m = m; g.n = cols - c1; g.k = c1;
     g.A = P + r0; g.lda = lda; g.transA = 0;
@@ -230,13 +269,19 @@ void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, in
     g.outLower = r0 < cols ? 1 : 0;
     gemm(h, g, cls);
   };
+  if (rows > split_row) {
+    fork_side(h);
+    h->on_side = true;
+    upd(split_row, rows - split_row, BULK);
+    h->on_side = false;
+  }
   if (h->split && h->opts.fp64_diag) {
     upd(c1, cols - c1, DIAG);              // inside the diagonal block: FP64 accuracy
-    if (rows > cols) upd(cols, rows - cols, BULK);
+    upd(cols, split_row - cols, BULK);
   } else {
-    upd(c1, rows - c1, BULK);
+    upd(c1, split_row - c1, BULK);
   }
-  panel_potrf(h, P + c1 + (long long)c1 * lda, lda, rows - c1, cols - c1, col0 + c1,
+  panel_potrf(h, P + c1 + (long long)c1 * lda, lda, rows - c1, cols - c1, dr - c1, col0 + c1,
               part0 + c1 / nb);
 }
 
@@ -257,20 +302,21 @@ void issue_factor(rgf_handle* h) {
     if (i > 0) {
       const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
       const long long ldm = mf_lda(sh, i - 1);
-      GemmDesc g;  // D_i -= L_{i,i-1} L_{i,i-1}^T   (RGF.H:276, 304)
-      g.m = g.n = g.k = (int)ns;
+      // [D_i; C_i] -= [L_{i,i-1}; C_{i-1}] L_{i,i-1}^T  (RGF.H:276, 279, 304, 307): the
+      // rows [L_{i,i-1}; C_{i-1}] are adjacent in block column i-1, so both
+      // updates run as one product (lower part only for D_i)
+      GemmDesc g;
+      g.m = (int)(ns + nd); g.n = g.k = (int)ns;
       g.A = Pm + ns; g.lda = ldm; g.B = Pm + ns; g.ldb = ldm; g.transB = 1;
       g.C = g.D = P; g.ldc = g.ldd = lda;
+      if (nd > 0) {
+        g.C2 = g.D2 = P + mf_dense_row(sh, i);
+        g.mD1 = (int)ns;
+      }
       g.alpha = -1.0; g.beta = 1.0; g.outLower = 1;
       gemm(h, g, BULK);
       if (nd > 0) {
         const double* Cm = Pm + mf_dense_row(sh, i - 1);
-        GemmDesc a;  // C_i -= C_{i-1} L_{i,i-1}^T  (RGF.H:279, 307)
-        a.m = (int)nd; a.n = (int)ns; a.k = (int)ns;
-        a.A = Cm; a.lda = ldm; a.B = Pm + ns; a.ldb = ldm; a.transB = 1;
-        a.C = a.D = P + mf_dense_row(sh, i); a.ldc = a.ldd = lda;
-        a.alpha = -1.0; a.beta = 1.0;
-        gemm(h, a, BULK);
         GemmDesc c;  // corner -= C_{i-1} C_{i-1}^T  (RGF.H:280, 308)
         c.m = c.n = (int)nd; c.k = (int)ns;
         c.A = Cm; c.lda = ldm; c.B = Cm; c.ldb = ldm; c.transB = 1;
@@ -279,7 +325,8 @@ void issue_factor(rgf_handle* h) {
         gemm(h, c, SMALL);
       }
     }
-    panel_potrf(h, P, lda, (int)lda, (int)ns, (int)(i * ns), (int)(i * tiles));
+    panel_potrf(h, P, lda, (int)lda, (int)ns, (int)ns, (int)(i * ns), (int)(i * tiles));
+    if (h->lookahead && h->side && lda > ns) join_side(h);
   }
   if (nd > 0) {
     const double* Pl = h->d_MF + mf_col_offset(sh, nt - 1);
@@ -290,7 +337,8 @@ void issue_factor(rgf_handle* h) {
     c.C = c.D = corner; c.ldc = c.ldd = nd;
     c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
     gemm(h, c, SMALL);
-    panel_potrf(h, corner, nd, (int)nd, (int)nd, (int)(nt * ns), (int)(nt * tiles));  // RGF.H:335
+    panel_potrf(h, corner, nd, (int)nd, (int)nd, (int)nd, (int)(nt * ns),
+                (int)(nt * tiles));  // RGF.H:335
   }
   launch_logdet_reduce(h->d_logpart, h->nparts, h->d_scalars, s);
   h->kernels_issued++;
@@ -389,38 +437,50 @@ void issue_selinv(rgf_handle* h) {
     const long long ldn = has_next ? mf_lda(sh, i + 1) : 0;
     const double* Sdn = has_next ? Sn + mf_dense_row(sh, i + 1) : nullptr;       // Sigma_{d,i+1}
     if (!compat) {
+      // Rows below the diagonal block are [L_{i+1,i}; C_i] = P + ns and
+      // [Sigma_{i+1,i}; Sigma_{d,i}] = Q + ns (adjacent), so the products that
+      // produce or consume them run once over ns + nd rows instead of as a
+      // square product plus a thin nd-row one.
       if (has_next) {
-        // X = Sigma_{i+1,i+1} L_{i+1,i} + Sigma_{d,i+1}^T C_i
-        gemm(h, mk(ins, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ns, 1.0, 0.0), BULK);
-        if (nd > 0)
-          gemm(h, mk(ins, ins, ind, Sdn, ldn, 1, Ci, lda, 0, h->d_T1, ns, h->d_T1, ns, 1.0, 1.0),
+        const int m2 = ins + ind;
+        const long long ldt = m2;
+        // [X; Y] = [Sigma_{i+1,i+1}; Sigma_{d,i+1}] L_{i+1,i}
+        //          + [Sigma_{d,i+1}^T C_i; Sigma_dd C_i]
+        GemmDesc x = mk(m2, ins, ins, Sn, ldn, 0, Bi, lda, 0, nullptr, 0, h->d_T1, ldt, 1.0, 0.0);
+        if (nd > 0) {
+          x.A2 = Sdn;
+          x.mA1 = ins;
+        }
+        gemm(h, x, BULK);
+        if (nd > 0) {
+          gemm(h, mk(ins, ins, ind, Sdn, ldn, 1, Ci, lda, 0, h->d_T1, ldt, h->d_T1, ldt, 1.0, 1.0),
                SMALL);
-        // Sigma_{i+1,i} = -X L_ii^{-1} = -X U_i^T
-        GemmDesc g = mk(ins, ins, ins, h->d_T1, ns, 0, Ui, ns, 1, nullptr, 0, Q + ns, lda, -1.0, 0.0);
+          gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, h->d_T1 + ns, ldt, h->d_T1 + ns, ldt,
+                     1.0, 1.0), SMALL);
+        }
+        // [Sigma_{i+1,i}; Sigma_{d,i}] = -[X; Y] L_ii^{-1} = -[X; Y] U_i^T
+        GemmDesc g = mk(m2, ins, ins, h->d_T1, ldt, 0, Ui, ns, 1, nullptr, 0, Q + ns, lda, -1.0, 0.0);
         g.triB = TRI_LOWER;
         gemm(h, g, BULK);
-      }
-      if (nd > 0) {
-        // Y = Sigma_dd C_i + Sigma_{d,i+1} L_{i+1,i};  Sigma_{d,i} = -Y U_i^T
-        gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0), SMALL);
-        if (has_next)
-          gemm(h, mk(ind, ins, ins, Sdn, ldn, 0, Bi, lda, 0, h->d_T3, nd, h->d_T3, nd, 1.0, 1.0),
-               BULK);
-        GemmDesc g = mk(ind, ins, ins, h->d_T3, nd, 0, Ui, ns, 1, nullptr, 0,
-                        Q + mf_dense_row(sh, i), lda, -1.0, 0.0);
-        g.triB = TRI_LOWER;
-        gemm(h, g, BULK);
-      }
-      // W^T = U_i - Sigma_{i+1,i}^T L_{i+1,i} - Sigma_{d,i}^T C_i
-      if (has_next) {
-        gemm(h, mk(ins, ins, ins, Q + ns, lda, 1, Bi, lda, 0, Ui, ns, h->d_T2, ns, -1.0, 1.0), BULK);
+        // W^T = U_i - [Sigma_{i+1,i}; Sigma_{d,i}]^T [L_{i+1,i}; C_i]
+        gemm(h, mk(ins, ins, m2, Q + ns, lda, 1, Bi, lda, 0, Ui, ns, h->d_T2, ns, -1.0, 1.0), BULK);
       } else {
-        launch_copy(Ui, ns, h->d_T2, ns, ins, ins, 1, 0, 0, s);
-        h->kernels_issued++;
+        if (nd > 0) {
+          // Y = Sigma_dd C_i;  Sigma_{d,i} = -Y U_i^T
+          gemm(h, mk(ind, ins, ind, Sdd, nd, 0, Ci, lda, 0, nullptr, 0, h->d_T3, nd, 1.0, 0.0),
+               SMALL);
+          GemmDesc g = mk(ind, ins, ins, h->d_T3, nd, 0, Ui, ns, 1, nullptr, 0,
+                          Q + mf_dense_row(sh, i), lda, -1.0, 0.0);
+          g.triB = TRI_LOWER;
+          gemm(h, g, BULK);
+          // W^T = U_i - Sigma_{d,i}^T C_i
+          gemm(h, mk(ins, ins, ind, Q + mf_dense_row(sh, i), lda, 1, Ci, lda, 0, Ui, ns, h->d_T2,
+                     ns, -1.0, 1.0), SMALL);
+        } else {
+          launch_copy(Ui, ns, h->d_T2, ns, ins, ins, 1, 0, 0, s);
+          h->kernels_issued++;
+        }
       }
-      if (nd > 0)
-        gemm(h, mk(ins, ins, ind, Q + mf_dense_row(sh, i), lda, 1, Ci, lda, 0, h->d_T2, ns,
-                   h->d_T2, ns, -1.0, 1.0), SMALL);
       // Sigma_ii = L_ii^{-T} W = U_i (W^T)^T
       GemmDesc g = mk(ins, ins, ins, Ui, ns, 0, h->d_T2, ns, 1, nullptr, 0, Q, lda, 1.0, 0.0);
       g.triA = TRI_UPPER;
@@ -542,7 +602,7 @@ int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, F issue) {
     issue();
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (e != cudaSuccess) return cuda_status(e);
-    e = cudaGraphInstantiate(exec, graph, 0);
+    e = cudaGraphInstantiateWithFlags(exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       *exec = nullptr;
@@ -612,7 +672,7 @@ int alloc_selinv(rgf_handle* h) {
   int st;
   if ((st = dalloc(h, &h->d_MS, h->mf_size))) return st;
   if ((st = dalloc(h, &h->d_U, nt * ns * ns + nd * nd))) return st;
-  if ((st = dalloc(h, &h->d_T1, ns * ns))) return st;
+  if ((st = dalloc(h, &h->d_T1, (ns + nd) * ns))) return st;
   if ((st = dalloc(h, &h->d_T2, ns * ns))) return st;
   if ((st = dalloc(h, &h->d_T3, std::max<long long>(1, nd * ns)))) return st;
   RGF_CK(cudaMemsetAsync(h->d_MS, 0, sizeof(double) * h->mf_size, h->stream));
@@ -649,10 +709,15 @@ void release(rgf_handle* h) {
   for (auto& e : h->ev_used) { cudaEventDestroy(e.e0); cudaEventDestroy(e.e1); }
   for (auto& e : h->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   delete h->split;
+  delete h->split_side;
   void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
                   h->d_logpart, h->d_scalars, h->d_diag, h->d_status, h->d_rhs, h->d_partial,
-                  h->d_res, h->d_gemm_ws};
+                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side};
   for (void* p : bufs) dfree(p);
+  if (h->side) cudaStreamSynchronize(h->side);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -726,10 +791,17 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
   h->mf_size = 2 * (long long)(nt - 1) * ns * ns + (long long)ns * ns + n * (long long)nd;
   int st = RGF_OK;
   do {
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // the main stream carries the critical path: give it the higher priority
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
       st = RGF_ECUDA;
       break;
     }
+    if (const char* e = std::getenv("RGF_GB300_LOOKAHEAD")) h->lookahead = std::atoi(e) != 0;
     if ((st = dalloc(h, &h->d_ia, n + 1))) break;
     if ((st = dalloc(h, &h->d_ja, h->nnz))) break;
     if ((st = dalloc(h, &h->d_a, h->nnz))) break;
@@ -747,6 +819,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     h->gemm_ws_elems = std::min<long long>(20ll << 20, 8ll * (2 * (long long)ns + (long long)nd) *
                                                            std::max<long long>(ns, nd));
     if ((st = dalloc(h, &h->d_gemm_ws, h->gemm_ws_elems))) break;
+    if ((st = dalloc(h, &h->d_gemm_ws_side, h->gemm_ws_elems))) break;
     if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice, h->stream) ||
         cudaMemcpyAsync(h->d_ja, ja, sizeof(size_t) * h->nnz, cudaMemcpyHostToDevice, h->stream) ||
         cudaMemcpyAsync(h->d_a, a, sizeof(double) * h->nnz, cudaMemcpyHostToDevice, h->stream)) {
@@ -756,8 +829,12 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     if (o.precision == RGF_PREC_SPLIT) {
       h->split = SplitEngine::create(o.slices, &st);
       if (st) break;
-      // operands have at most 2ns+nd rows and ns (or nd) terms
-      st = h->split->prepare((int)(2 * ns + nd), (int)std::max(ns, nd), (int)nt);
+      // operands have at most 2ns+nd rows and ns+nd terms
+      st = h->split->prepare((int)(2 * ns + nd), (int)(ns + nd), (int)nt);
+      if (st) break;
+      h->split_side = SplitEngine::create(o.slices, &st);
+      if (st) break;
+      st = h->split_side->prepare((int)(ns + nd), (int)ns, 1);
       if (st) break;
     }
     // validate the pattern once on the device

@@ -25,6 +25,13 @@ enum Tri { TRI_NONE = 0, TRI_LOWER = 1, TRI_UPPER = 2 };
 struct GemmDesc {
   int m = 0, n = 0, k = 0;
   const double* A = nullptr; long long lda = 0; int transA = 0;
+  // Rows >= mA1 of A come from A2 (row r at A2 + (r - mA1), same lda and
+  // batch stride): a stacked operand whose two row blocks are not adjacent
+  // in memory.  transA == 0 only; A2 == nullptr means one block.
+  const double* A2 = nullptr; int mA1 = 0;
+  // Rows >= mD1 of C and D live at C2 / D2 (row r at D2 + (r - mD1), same
+  // leading dimensions and batch strides); D2 == nullptr means one block.
+  const double* C2 = nullptr; double* D2 = nullptr; int mD1 = 0;
   const double* B = nullptr; long long ldb = 0; int transB = 0;
   const double* C = nullptr; long long ldc = 0;
   double* D = nullptr; long long ldd = 0;

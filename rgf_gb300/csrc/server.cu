@@ -30,6 +30,7 @@ struct Factor {
   rgf_handle* h = nullptr;
   size_t bytes = 0;
   bool busy = false;
+  int pending = 0;  // queued solve / diag requests that name this factor
   Clock::time_point last_use;
 };
 
@@ -37,6 +38,7 @@ struct Pending {
   rgf_request* req;
   long long ticket;
   Clock::time_point t_submit;
+  bool pinned;  // holds one `pending` reference on its factor
 };
 
 size_t estimate_bytes(const rgf_opts& o, size_t ns, size_t nt, size_t nd, size_t nnz) {
@@ -44,11 +46,14 @@ size_t estimate_bytes(const rgf_opts& o, size_t ns, size_t nt, size_t nd, size_t
   const size_t mf = 2 * (nt - 1) * ns * ns + ns * ns + n * nd;
   size_t b = 16 * nnz + 8 * (n + 1) + 8 * mf;       // CSC + factor
   b += 8 * mf + 8 * (nt * ns * ns + nd * nd) + 8 * (2 * ns * ns + nd * ns);  // selected inverse
-  b += 8 * std::min<size_t>(20u << 20, 8 * (2 * ns + nd) * std::max(ns, nd));
-  if (o.precision == RGF_PREC_SPLIT) {
-    const size_t r = (2 * ns + nd + 127) / 128 * 128, k = (std::max(ns, nd) + 63) / 64 * 64;
+  // split-K workspaces of the main and side streams
+  b += 2 * 8 * std::min<size_t>(20u << 20, 8 * (2 * ns + nd) * std::max(ns, nd));
+  if (o.precision == RGF_PREC_SPLIT) {  // slice workspaces of the main and side streams
+    const size_t r = (2 * ns + nd + 127) / 128 * 128, k = (ns + nd + 63) / 64 * 64;
     const size_t one = 2 * 8 * r * k * 2;
     b += std::max(one, std::min<size_t>((size_t)1 << 30, nt * one / 4)) + (1 << 20);
+    const size_t r2 = (ns + nd + 127) / 128 * 128;
+    b += 2 * 8 * r2 * k * 2 + (1 << 20);
   }
   return b + (8u << 20);
 }
@@ -71,13 +76,15 @@ struct rgf_server {
 
 namespace {
 
-// Evict least-recently-used idle factors until `need` more bytes fit.
+// Evict least-recently-used idle factors until `need` more bytes fit.  A
+// factor that a queued request names is not idle: it stays resident until
+// that request has run.
 bool make_room(rgf_server* s, size_t need) {
   while (s->used + need > s->budget) {
     long long victim = 0;
     Clock::time_point oldest = Clock::time_point::max();
     for (auto& kv : s->factors)
-      if (!kv.second.busy && kv.second.last_use < oldest) {
+      if (!kv.second.busy && kv.second.pending == 0 && kv.second.last_use < oldest) {
         oldest = kv.second.last_use;
         victim = kv.first;
       }
@@ -157,6 +164,7 @@ void run_request(rgf_server* s, Pending p) {
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->factors.find(r->factor_id);
     if (it != s->factors.end()) {
+      if (p.pinned) it->second.pending--;
       if (r->kind == RGF_REQ_RELEASE && !st) {
         s->used -= it->second.bytes;
         rgf_destroy(it->second.h);
@@ -188,6 +196,8 @@ void worker(rgf_server* s) {
     Pending p = s->queue[i];
     s->queue.erase(s->queue.begin() + i);
     s->stats.admitted++;
+    if (p.pinned && p.req->kind != RGF_REQ_FACTOR && !s->factors.count(p.req->factor_id))
+      p.pinned = false;  // released before this request ran
     lk.unlock();
     run_request(s, p);
     lk.lock();
@@ -219,7 +229,15 @@ int rgf_server_submit(rgf_server* s, rgf_request* r, long long* ticket) {
   r->latency_ms = 0.0;
   r->reserved_bytes = 0;
   *ticket = s->next_ticket++;
-  s->queue.push_back({r, *ticket, Clock::now()});
+  bool pinned = false;
+  if (r->kind != RGF_REQ_FACTOR) {
+    auto it = s->factors.find(r->factor_id);
+    if (it != s->factors.end()) {
+      it->second.pending++;
+      pinned = true;
+    }
+  }
+  s->queue.push_back({r, *ticket, Clock::now(), pinned});
   s->stats.submitted++;
   s->cv_work.notify_one();
   return RGF_OK;

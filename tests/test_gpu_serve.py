@@ -70,3 +70,24 @@ def test_eviction_and_release(rgf):
     rel = srv.wait(srv.submit_release(f2["factor_id"]))
     assert rel["status"] == 0 and srv.stats()["resident_factors"] == 0
     srv.close()
+
+
+def test_queued_request_keeps_its_factor_resident(rgf):
+    """A diag queued on a factor pins it: a factorization that needs its memory
+    waits until the diag has run, then evicts it."""
+    ns, nt, nd = 200, 3, 2
+    m1 = gen.generate_bta(ns, nt, nd, seed=1)
+    m2 = gen.generate_bta(ns, nt, nd, seed=2)
+    srv = rgf.RGFServer(hbm_budget_bytes=30 << 20, slots=2)
+    f1 = srv.wait(srv.submit_factor(*m1, ns, nt, nd))
+    assert f1["status"] == 0
+    td = [srv.submit_diag(f1["factor_id"], ns * nt + nd) for _ in range(3)]
+    tf = srv.submit_factor(*m2, ns, nt, nd)
+    diags = [srv.wait(t) for t in td]
+    f2 = srv.wait(tf)
+    assert all(d["status"] == 0 for d in diags) and f2["status"] == 0
+    assert srv.stats()["evicted"] == 1
+    alone = rgf.RGF(*m1, ns, nt, nd)
+    assert np.array_equal(diags[0]["diag"], alone.RGFdiag())
+    alone.close()
+    srv.close()
