@@ -457,18 +457,25 @@ def run_rgf(args, w):
 
     # end-to-end through the public API: host CSC -> device, diag -> host
     e2e_ms = []
+    e2e_parts = None
     for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
                           slices=args.slices, device=dev, fp64_diag=not args.no_fp64_diag)
+        t1 = time.perf_counter()
         h.factorize()
+        t2 = time.perf_counter()
         h.logDet()
         h.RGFdiag(diag_host)
+        t3 = time.perf_counter()
         h.close()
-        dt = (time.perf_counter() - t0) * 1e3
+        t4 = time.perf_counter()
+        dt = (t4 - t0) * 1e3
         if i > 0:
             e2e_ms.append(dt)
+            e2e_parts = {"create_h2d_ms": (t1 - t0) * 1e3, "factorize_ms": (t2 - t1) * 1e3,
+                         "logdet_rgfdiag_d2h_ms": (t3 - t2) * 1e3, "destroy_ms": (t4 - t3) * 1e3}
     e2e_med = statistics.median(e2e_ms) if e2e_ms else float("nan")
     if dist and e2e_ms:
         t = torch.tensor([max(e2e_ms)], dtype=torch.float64, device="cuda")
@@ -548,7 +555,7 @@ def run_rgf(args, w):
                                h2d / 1e9, s.info()["mf_size"] * 8 / 1e9)},
                 "e2e": ({"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
                          "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
-                         "d2h_bytes_per_step": d2h} if e2e_ms else None),
+                         "d2h_bytes_per_step": d2h, "parts": e2e_parts} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
                 "plain_fp64": plain,
                 "clocks": clk, "logdet": logdet,

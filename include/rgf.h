@@ -47,14 +47,14 @@ enum rgf_selinv_mode {
 
 typedef struct rgf_opts {
   int precision;    /* enum rgf_precision (default RGF_PREC_FP64)             */
-  int slices;       /* split precision: 7-bit slices per operand (1..8),
-                       0 = default 6 (42-bit operands)                        */
+  int slices;       /* split precision: 8-bit slices per operand (1..8),
+                       0 = default 5 (40-bit operands)                        */
   int selinv_mode;  /* enum rgf_selinv_mode (default RGF_SELINV_EXACT)        */
   int device;       /* CUDA device ordinal, -1 = the current device           */
   int use_graphs;   /* 1 = replay each stage as a captured CUDA graph         */
   int fp64_diag;    /* split precision, Cholesky and inverse of the diagonal
                        blocks: 1 (default) FP64 accuracy, their inner products
-                       emulated with 8 slices (56-bit operands); 2 native FP64
+                       emulated with 7 slices (56-bit operands); 2 native FP64
                        units; 0 the bulk slice count                          */
   int reserved[10];
 } rgf_opts;

@@ -2,20 +2,26 @@
 //
 // D = alpha * op(A) * op(B) + beta * C with FP64 operands:
 //  1. every row r of op(A) is scaled by 2^-ea[r] (|x| < 2^ea[r]) and cut into
-//     S base-2^beta digits (integers |d| < 2^beta, exact in bf16); every column
-//     c of op(B) likewise with 2^-eb[c].  The cut is done on the FP64 bit
-//     pattern with integer instructions only (no FP64 arithmetic).
+//     S balanced base-2^8 digits (integers in [-128, 128], exact in bf16;
+//     8S - 1 bits of the row's magnitude); every column c of op(B) likewise
+//     with 2^-eb[c].  The cut is done on the FP64 bit pattern with integer
+//     instructions only (no FP64 arithmetic).
 //  2. for every digit pair (s, t) with s + t <= S + 1 the tensor cores form
 //     the integer products P_st = A_s B_t in FP32 in tensor memory.  Pairs of
-//     one level (s + t) share an accumulator; a job sums the level's pairs over
-//     a K range of at most 1024 terms in total, so with beta = 7 every sum is
-//     below 2^24 and thus exact;
+//     one level (s + t) accumulate together; a job sums a level's pairs over
+//     a K range of at most 1024 terms in total, so every sum of products
+//     (each at most 2^14) is below 2^24 and thus exact;
 //  3. each exact partial is moved to registers and added, shifted by its
 //     level, into a 64-bit integer fixed-point accumulator (integer sums: the
 //     result does not depend on how terms are grouped into jobs);
 //  4. one conversion to FP64 per output, scaled by 2^(ea[r] + eb[c] + ...).
+// With both operands read from shared memory the tensor cores are fed at
+// about 64 bytes per cycle per SM, so the cost is the number of slice-pair
+// MMAs: 8-bit digits need 15 pairs for 39-bit operands where 7-bit digits
+// need 21 for 42 bits.
 // The GEMM kernel is warp specialized: one warp issues TMA tile loads
-// (cp.async.bulk.tensor, 128B swizzle) into a 4-stage shared-memory ring, one
+// (cp.async.bulk.tensor, 128B swizzle, 128 K terms per stage as two swizzle
+// atoms) into a 3-stage shared-memory ring, one
 // elected thread issues tcgen05.mma (M=128, N=128, K=16, bf16 -> f32) into
 // two TMEM accumulators, and eight warps drain the accumulators while the next
 // product accumulates.  Every wait on an mbarrier is bounded; a wait that
@@ -37,14 +43,15 @@ namespace rgf {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BKE = 64;  // tile rows, cols, K elements per stage
-#ifndef RGF_SPLIT_NSTAGE
-#define RGF_SPLIT_NSTAGE 4
-#endif
-constexpr int NSTAGE = RGF_SPLIT_NSTAGE;
-constexpr int KCHUNK_BLOCKS = 16;             // 16 x 64 = 1024 terms per exact FP32 sum
-constexpr int SPLIT_BETA = 7;
+constexpr int BM = 128, BN = 128, BKE = 64;  // tile rows, cols, K elements per swizzle atom
+constexpr int ATOMS = 2;                      // atoms per pipeline stage
+constexpr int SBK = BKE * ATOMS;              // K terms per stage
+constexpr int NSTAGE = 3;
+constexpr int SPLIT_BETA = 8;
+// terms per exact FP32 sum: 2^24 / 2^(2 beta - 2) (balanced digits, products <= 2^14)
+constexpr int EXACT_TERMS = 1 << (24 - 2 * SPLIT_BETA + 2);
 constexpr int MAXPAIRS = 45;
+constexpr int MAXGROUPS = 48;
 constexpr int NUM_THREADS = 320;              // warp 0 TMA, warp 1 MMA, warps 2..9 drain
 constexpr uint32_t TILE_BYTES = BM * BKE * 2; // 16 KiB per operand tile
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any mbarrier wait
@@ -54,6 +61,10 @@ struct SplitParams {
   int S, beta, cs;
   int npairs;
   unsigned char ps[MAXPAIRS], pt[MAXPAIRS];
+  // pair groups: pairs g0 .. g0 + gs - 1 (one level, glevel = s + t - 2)
+  // accumulate together over gchunk stages at a time
+  int ngroups;
+  unsigned char g0[MAXGROUPS], gs[MAXGROUPS], glevel[MAXGROUPS], gchunk[MAXGROUPS];
   int triA, triB, outLower;
   const int* exA;
   const int* exB;
@@ -193,13 +204,9 @@ __device__ __forceinline__ void tile_kblocks(const SplitParams& p, int m0, int n
   if (p.triA == TRI_UPPER) lo = max(lo, m0);
   if (p.triB == TRI_LOWER) lo = max(lo, n0);
   if (p.triB == TRI_UPPER) hi = min(hi, n0 + BN);
-  kb_lo = lo / BKE;
-  kb_hi = hi > lo ? (hi + BKE - 1) / BKE : kb_lo;
+  kb_lo = lo / SBK;
+  kb_hi = hi > lo ? (hi + SBK - 1) / SBK : kb_lo;
 }
-
-// K blocks per job at level l (l + 1 pairs share the accumulator): at most
-// 1024 product terms per exact FP32 sum.
-__device__ __forceinline__ int level_chunk(int l) { return max(1, KCHUNK_BLOCKS / (l + 1)); }
 
 // ---- the slice-product GEMM ---------------------------------------------------
 __global__ void __launch_bounds__(NUM_THREADS, 1)
@@ -208,9 +215,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
-  uint8_t* tilesA = smem;                                  // NSTAGE x 16 KiB
-  uint8_t* tilesB = smem + NSTAGE * TILE_BYTES;            // NSTAGE x 16 KiB
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 2 * NSTAGE * TILE_BYTES);
+  uint8_t* tilesA = smem;                                  // NSTAGE x ATOMS x 16 KiB
+  uint8_t* tilesB = smem + NSTAGE * ATOMS * TILE_BYTES;    // NSTAGE x ATOMS x 16 KiB
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 2 * NSTAGE * ATOMS * TILE_BYTES);
   uint64_t* empty = full + NSTAGE;
   uint64_t* acc_full = empty + NSTAGE;                     // 2 accumulators
   uint64_t* acc_empty = acc_full + 2;
@@ -226,10 +233,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   int kb_lo, kb_hi;
   tile_kblocks(p, m0, n0, kb_lo, kb_hi);
   const int nkb = kb_hi - kb_lo;
-  // jobs: for each level l (pairs l*(l+1)/2 .. +l), K chunks of
-  // KCHUNK_BLOCKS / (l + 1) blocks (1024 terms over the level's pairs)
+  // jobs: for each pair group, K chunks of gchunk stages
   int njobs = 0;
-  for (int l = 0; l < p.S; ++l) njobs += nkb > 0 ? (nkb + level_chunk(l) - 1) / level_chunk(l) : 0;
+  for (int g = 0; g < p.ngroups; ++g) njobs += nkb > 0 ? (nkb + p.gchunk[g] - 1) / p.gchunk[g] : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
@@ -259,18 +265,23 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     if (lane == 0) {
       long long use = 0;
       bool ok = true;
-      for (int l = 0; l < p.S && ok; ++l) {
-        const int chunk = level_chunk(l), p0 = l * (l + 1) / 2;
+      for (int g = 0; g < p.ngroups && ok; ++g) {
+        const int chunk = p.gchunk[g], p0 = p.g0[g], p1 = p0 + p.gs[g];
         for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk) {
           const int kb1 = min(kb_hi, kb0 + chunk);
-          for (int pr = p0; pr <= p0 + l && ok; ++pr)
+          for (int pr = p0; pr < p1 && ok; ++pr)
             for (int kb = kb0; kb < kb1; ++kb, ++use) {
               const int s = (int)(use % NSTAGE);
               const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
               if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, p.st)) { ok = false; break; }
-              mbar_expect_tx(&full[s], 2 * TILE_BYTES);
-              tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], kb * BKE, m0, zS + p.ps[pr]);
-              tma_load_3d(tilesB + s * TILE_BYTES, &tmB, &full[s], kb * BKE, n0, zS + p.pt[pr]);
+              mbar_expect_tx(&full[s], 2 * ATOMS * TILE_BYTES);
+              for (int at = 0; at < ATOMS; ++at) {  // K beyond the slices' extent reads zeros
+                const int x = kb * SBK + at * BKE;
+                tma_load_3d(tilesA + (s * ATOMS + at) * TILE_BYTES, &tmA, &full[s], x, m0,
+                            zS + p.ps[pr]);
+                tma_load_3d(tilesB + (s * ATOMS + at) * TILE_BYTES, &tmB, &full[s], x, n0,
+                            zS + p.pt[pr]);
+              }
             }
         }
       }
@@ -286,8 +297,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       long long use = 0;
       int j = 0;
       bool ok = true;
-      for (int l = 0; l < p.S && ok; ++l) {
-        const int chunk = level_chunk(l);
+      for (int g = 0; g < p.ngroups && ok; ++g) {
+        const int chunk = p.gchunk[g], npr = p.gs[g];
         for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk, ++j) {
           const int kb1 = min(kb_hi, kb0 + chunk);
           const int buf = j & 1;
@@ -296,18 +307,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           tc_fence_after();
           const uint32_t tacc = tmem_base + (uint32_t)(buf * BN);
           bool first = true;
-          for (int pr = 0; pr <= l && ok; ++pr)
+          for (int pr = 0; pr < npr && ok; ++pr)
             for (int kb = kb0; kb < kb1; ++kb, ++use) {
               const int s = (int)(use % NSTAGE);
               const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
               if (!mbar_wait(&full[s], ph, abort_flag, p.st)) { ok = false; break; }
               tc_fence_after();
-              const uint64_t ad = smem_desc_sw128(tilesA + s * TILE_BYTES);
-              const uint64_t bd = smem_desc_sw128(tilesB + s * TILE_BYTES);
 #pragma unroll
-              for (int kk = 0; kk < BKE / 16; ++kk) {  // +32 bytes per K=16 step in the swizzle atom
-                umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2), first ? 0u : 1u);
-                first = false;
+              for (int at = 0; at < ATOMS; ++at) {
+                const uint64_t ad = smem_desc_sw128(tilesA + (s * ATOMS + at) * TILE_BYTES);
+                const uint64_t bd = smem_desc_sw128(tilesB + (s * ATOMS + at) * TILE_BYTES);
+#pragma unroll
+                for (int kk = 0; kk < BKE / 16; ++kk) {  // +32 bytes per K=16 step in the atom
+                  umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2),
+                            first ? 0u : 1u);
+                  first = false;
+                }
               }
               umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
@@ -329,19 +344,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     long long acc[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) acc[i] = 0;
-    int l = 0, jl = 0;  // level of job j and job index within the level
-    const int nch0 = nkb > 0 ? (nkb + level_chunk(0) - 1) / level_chunk(0) : 0;
-    int nch = nch0;
-    for (int j = 0; j < njobs; ++j, ++jl) {
-      while (jl >= nch) {
-        ++l;
-        jl = 0;
-        nch = (nkb + level_chunk(l) - 1) / level_chunk(l);
+    int g = 0, jg = 0;  // group of job j and job index within the group
+    int nch = nkb > 0 && p.ngroups > 0 ? (nkb + p.gchunk[0] - 1) / p.gchunk[0] : 0;
+    for (int j = 0; j < njobs; ++j, ++jg) {
+      while (jg >= nch) {
+        ++g;
+        jg = 0;
+        nch = (nkb + p.gchunk[g] - 1) / p.gchunk[g];
       }
       const int buf = j & 1;
       if (!mbar_wait(&acc_full[buf], (uint32_t)((j >> 1) & 1), abort_flag, p.st)) break;
       tc_fence_after();
-      const int sh = p.beta * (p.S - 1 - l) - p.cs;
+      const int sh = p.beta * (p.S - 1 - p.glevel[g]) - p.cs;
       const uint32_t taddr =
           tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + half * 64);
 #pragma unroll
@@ -351,7 +365,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const long long v = (long long)__float2int_rn(__uint_as_float(r[i]));
-          acc[part * 16 + i] += sh >= 0 ? (v << sh) : (v >> (-sh));
+          acc[part * 16 + i] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
         }
       }
       tc_fence_before();
@@ -366,7 +380,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const double* C = hi ? p.C2 + (long long)zb * p.sC - p.mD1
                            : (p.C ? p.C + (long long)zb * p.sC : nullptr);
       double* D = hi ? p.D2 + (long long)zb * p.sD - p.mD1 : p.D + (long long)zb * p.sD;
-      const int er = p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1);
+      const int er = p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1) + 2;
       const int cbase = n0 + half * 64;
 #pragma unroll
       for (int i = 0; i < 64; ++i) {
@@ -393,6 +407,34 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 // triangle.  ex[r] = smallest e with |x| < 2^e over the row (0 for a zero row).
 __device__ __forceinline__ bool tri_ok(int tri, int r, int k) {
   return tri == TRI_NONE || (tri == TRI_LOWER ? k <= r : k >= r);
+}
+
+// Balanced base-2^beta digits of x * 2^(beta*S - 1 - e) (truncated to an
+// integer, |.| < 2^(beta*S - 1)): S digits, most significant first, the top
+// one in [-2^(beta-1), 2^(beta-1)] and the others in [-2^(beta-1),
+// 2^(beta-1) - 1], written to S planes `plane` elements apart.  With beta = 8
+// every digit is exact in bf16 and every digit product is at most 2^14.
+__device__ __forceinline__ void write_digits(unsigned long long bits, int e, int S, int beta,
+                                             __nv_bfloat16* o, size_t plane) {
+  const bool neg = (bits >> 63) != 0;
+  int E = (int)((bits >> 52) & 0x7ff);
+  unsigned long long mant = bits & 0xfffffffffffffull;
+  if (E) mant |= 1ull << 52; else E = 1;
+  const int sh = (E - 1075) + beta * S - 1 - e;
+  unsigned long long xi = 0;
+  if (mant != 0) {
+    if (sh >= 0) xi = sh < 64 ? (mant << sh) : 0ull;
+    else xi = -sh < 64 ? (mant >> (-sh)) : 0ull;
+  }
+  long long v = neg ? -(long long)xi : (long long)xi;
+  const int half = 1 << (beta - 1), mask = (1 << beta) - 1;
+  for (int s = S - 1; s > 0; --s) {
+    int d = (int)v & mask;
+    d -= d >= half ? mask + 1 : 0;
+    v = (v - d) >> beta;
+    o[(size_t)s * plane] = __float2bfloat16_rn((float)d);
+  }
+  o[0] = __float2bfloat16_rn((float)(int)v);
 }
 
 __device__ __forceinline__ int exp_of_max(unsigned long long mx) {
@@ -477,29 +519,12 @@ __global__ void slice_kernel(const double* X, long long rs, long long ks, int R,
     tile[rl][kl] = v;
   }
   __syncthreads();
-  const unsigned long long dmask = (1ull << beta) - 1ull;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int rl = ty + 8 * i, r = r0 + rl, k = k0 + tx;
     if (r >= Rp || k >= Kp) continue;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(tile[rl][tx]);
-    const bool neg = (b >> 63) != 0;
-    int E = (int)((b >> 52) & 0x7ff);
-    unsigned long long mant = b & 0xfffffffffffffull;
-    if (E) mant |= 1ull << 52; else E = 1;
-    // x * 2^(beta*S - ex[r]) as an integer, truncated: mant * 2^sh
-    const int sh = (E - 1075) + beta * S - (r < R ? ex[r] : 0);
-    unsigned long long xi = 0;
-    if (mant != 0) {
-      if (sh >= 0) xi = sh < 64 ? (mant << sh) : 0ull;
-      else xi = -sh < 64 ? (mant >> (-sh)) : 0ull;
-    }
-    const size_t plane = (size_t)Rp * Kp;
-    __nv_bfloat16* o = out + (size_t)r * Kp + k;
-    for (int s = 0; s < S; ++s) {
-      const int d = (int)((xi >> (beta * (S - 1 - s))) & dmask);
-      o[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
-    }
+    write_digits((unsigned long long)__double_as_longlong(tile[rl][tx]), r < R ? ex[r] : 0, S,
+                 beta, out + (size_t)r * Kp + k, (size_t)Rp * Kp);
   }
 }
 
@@ -575,7 +600,6 @@ __global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOp
   __syncthreads();
   // pass 2: digits, one 32 x 32 tile at a time (read along the contiguous
   // dimension, write along k)
-  const unsigned long long dmask = (1ull << beta) - 1ull;
   const size_t plane = (size_t)o.Rp * Kp;
   for (int k0 = 0; k0 < Kp; k0 += 32) {
 #pragma unroll
@@ -590,22 +614,8 @@ __global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOp
     for (int i = 0; i < 4; ++i) {
       const int rl = ty + 8 * i, r = r0 + rl, k = k0 + tx;
       if (r >= o.Rp) continue;
-      const unsigned long long bits = (unsigned long long)__double_as_longlong(tile[rl][tx]);
-      const bool neg = (bits >> 63) != 0;
-      int E = (int)((bits >> 52) & 0x7ff);
-      unsigned long long mant = bits & 0xfffffffffffffull;
-      if (E) mant |= 1ull << 52; else E = 1;
-      const int sh = (E - 1075) + beta * S - exs[rl];
-      unsigned long long xi = 0;
-      if (mant != 0) {
-        if (sh >= 0) xi = sh < 64 ? (mant << sh) : 0ull;
-        else xi = -sh < 64 ? (mant >> (-sh)) : 0ull;
-      }
-      __nv_bfloat16* q = out + (size_t)r * Kp + k;
-      for (int s = 0; s < S; ++s) {
-        const int d = (int)((xi >> (beta * (S - 1 - s))) & dmask);
-        q[s * plane] = __float2bfloat16_rn((float)(neg ? -d : d));
-      }
+      write_digits((unsigned long long)__double_as_longlong(tile[rl][tx]), exs[rl], S, beta,
+                   out + (size_t)r * Kp + k, plane);
     }
     __syncthreads();
   }
@@ -643,7 +653,7 @@ bool make_map(CUtensorMap* map, void* base, int S, int Rp, int Kp) {
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-constexpr size_t SMEM_BYTES = 1024 + 2 * NSTAGE * TILE_BYTES + 256;
+constexpr size_t SMEM_BYTES = 1024 + 2 * NSTAGE * ATOMS * TILE_BYTES + 256;
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
@@ -662,7 +672,7 @@ SplitEngine* SplitEngine::create(int slices, int* status) {
     return nullptr;
   }
   SplitEngine* e = new SplitEngine();
-  e->slices_ = slices > 0 ? slices : 6;
+  e->slices_ = slices > 0 ? slices : 5;
   e->min_k_ = 64;
   return e;
 }
@@ -735,8 +745,8 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
   std::memset(&p, 0, sizeof(p));
   p.m = g.m; p.n = g.n; p.k = g.k;
   p.S = S; p.beta = beta;
-  // bound of the fixed-point accumulator: K * 2^(beta*(S+1)) * 1.03 must stay below 2^62
-  const double lg = std::log2((double)g.k * 1.03) + beta * (S + 1);
+  // bound of the fixed-point accumulator: K * 2^(beta*(S+1) - 2) * 1.03 must stay below 2^62
+  const double lg = std::log2((double)g.k * 1.03) + beta * (S + 1) - 2;
   p.cs = std::max(0, (int)std::ceil(lg) - 62);
   int np = 0;
   for (int lvl = 2; lvl <= S + 1; ++lvl)
@@ -749,6 +759,24 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       }
     }
   p.npairs = np;
+  // groups: a level's pairs in groups of at most G, G * SBK terms per exact sum
+  {
+    const int G = std::max(1, EXACT_TERMS / SBK);
+    int ng = 0, off = 0;
+    for (int l = 0; l < S; ++l) {
+      const int cnt = l + 1, parts = (cnt + G - 1) / G;
+      for (int q = 0; q < parts && ng < MAXGROUPS; ++q) {
+        const int sz = cnt / parts + (q < cnt % parts ? 1 : 0);
+        p.g0[ng] = (unsigned char)off;
+        p.gs[ng] = (unsigned char)sz;
+        p.glevel[ng] = (unsigned char)l;
+        p.gchunk[ng] = (unsigned char)std::max(1, G / sz);
+        off += sz;
+        ++ng;
+      }
+    }
+    p.ngroups = ng;
+  }
   p.triA = g.triA; p.triB = g.triB; p.outLower = g.outLower;
   p.ldc = g.ldc; p.ldd = g.ldd; p.sC = g.sC; p.sD = g.sD;
   p.alpha = g.alpha; p.betac = g.beta;
@@ -833,7 +861,7 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       for (int bx = 0; bx < (int)grid.x; ++bx)
         for (int by = 0; by < (int)grid.y; ++by)
           if (!(g.outLower && bx * BM + BM <= by * BN)) tiles += 1.0;
-      *tensor_flops += tiles * nbat * 2.0 * BM * BN * (double)Kp * np;
+      *tensor_flops += tiles * nbat * 2.0 * BM * BN * (double)round_up(Kp, SBK) * np;
     }
     split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, p);
     launched += 1;

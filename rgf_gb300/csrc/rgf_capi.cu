@@ -73,6 +73,8 @@ struct rgf_handle {
   cudaGraphExec_t g_factor = nullptr, g_selinv = nullptr;
   long long k_factor = 0, k_selinv = 0;
   std::map<size_t, std::pair<cudaGraphExec_t, long long>> g_solve;
+  int runs_factor = 0, runs_selinv = 0;  // stage runs so far (the first one is not captured)
+  std::map<size_t, int> runs_solve;
   long long kernels_issued = 0;   // kernels of the stage being recorded
   long long kernels_total = 0;    // kernels launched over the handle's life
 
@@ -159,11 +161,11 @@ void join_side(rgf_handle* h) {
 void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
   const bool bulk = cls != SMALL;
-  // fp64_diag: 0 = diagonal blocks at the bulk slice count, 1 = at 8 slices
+  // fp64_diag: 0 = diagonal blocks at the bulk slice count, 1 = at 7 slices
   // (56-bit operands: FP64-accurate emulation), 2 = native FP64 DMMA
   const int fd = h->opts.fp64_diag;
   const bool may_split = cls == BULK || (cls == DIAG && fd != 2);
-  const int slices = (cls == DIAG && fd == 1) ? 8 : 0;
+  const int slices = (cls == DIAG && fd == 1) ? 7 : 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (h->timer_on && bulk) {
     if (h->ev_pool.empty()) {
@@ -191,7 +193,7 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
     auto up = [](double x, double m) { return std::ceil(x / m) * m; };
     // short K: both operands sliced in one launch
     const double fixed = up(g.k, 64) <= 512 ? 15e-6 : (g.A == g.B ? 40e-6 : 70e-6);
-    const double t_split = fixed + pairs * 2.0 * up(g.m, 128) * up(g.n, 128) * up(g.k, 64) *
+    const double t_split = fixed + pairs * 2.0 * up(g.m, 128) * up(g.n, 128) * up(g.k, 128) *
                                        g.batch / 700e12;
     const double t_fp64 = 8e-6 + gemm_flops(g) / 0.8e12;
     split = t_split < t_fp64;
@@ -586,9 +588,13 @@ void issue_solve(rgf_handle* h, int nrhs) {
 }
 
 // ---- graph capture / replay ----
+// The first run of a stage launches its kernels directly; from the second run
+// on, the stage is captured once into a CUDA graph and replayed.  A handle
+// used once (create, factorize, RGFdiag, destroy) never pays for a capture
+// and instantiation of tens of thousands of nodes.
 template <class F>
-int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, F issue) {
-  if (h->timer_on || !h->opts.use_graphs) {
+int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, int* runs, F issue) {
+  if (h->timer_on || !h->opts.use_graphs || (!*exec && (*runs)++ == 0)) {
     h->kernels_issued = 0;
     issue();
     h->kernels_total += h->kernels_issued;
@@ -657,7 +663,7 @@ int sync_and_check(rgf_handle* h) {
 
 int ensure_factored(rgf_handle* h) {
   if (h->factored) return RGF_OK;
-  int st = run_stage(h, &h->g_factor, &h->k_factor, [&] { issue_factor(h); });
+  int st = run_stage(h, &h->g_factor, &h->k_factor, &h->runs_factor, [&] { issue_factor(h); });
   if (st) return st;
   st = sync_and_check(h);
   if (st) return st;
@@ -684,7 +690,7 @@ int ensure_selinv(rgf_handle* h) {
   if (st) return st;
   if (h->selinv_done) return RGF_OK;
   if ((st = alloc_selinv(h))) return st;
-  st = run_stage(h, &h->g_selinv, &h->k_selinv, [&] { issue_selinv(h); });
+  st = run_stage(h, &h->g_selinv, &h->k_selinv, &h->runs_selinv, [&] { issue_selinv(h); });
   if (st) return st;
   st = sync_and_check(h);
   if (st) return st;
@@ -924,7 +930,7 @@ int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
   auto it = h->g_solve.find(nrhs);
   cudaGraphExec_t exec = it == h->g_solve.end() ? nullptr : it->second.first;
   long long nk = it == h->g_solve.end() ? 0 : it->second.second;
-  st = run_stage(h, &exec, &nk, [&] { issue_solve(h, (int)nrhs); });
+  st = run_stage(h, &exec, &nk, &h->runs_solve[nrhs], [&] { issue_solve(h, (int)nrhs); });
   if (st) return st;
   if (exec) h->g_solve[nrhs] = {exec, nk};
   RGF_CK(cudaMemcpyAsync(x, h->d_rhs, sizeof(double) * need, cudaMemcpyDeviceToHost, h->stream));

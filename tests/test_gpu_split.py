@@ -1,8 +1,8 @@
 """Split-precision (Ozaki, bf16 slices on tcgen05) GEMM and solver parity.
 
 The split GEMM is checked against the FP64 DMMA kernel and numpy on the same
-device operands: every entry within 1e-11 of (|A||B|)_{rc}, the bound of a
-42-bit (6 slices x 7 bits) split.  The solver in split precision is checked
+device operands: every entry within 2e-11 of (|A||B|)_{rc}, the bound of a
+40-bit (5 slices x 8 bits) split.  The solver in split precision is checked
 against the FP64 oracle at the split tolerances: logDet relative error
 <= 1e-9, RGFdiag max relative error <= 1e-8.
 """
@@ -14,7 +14,7 @@ from rgf_gb300 import gen
 
 pytestmark = pytest.mark.gpu
 
-GEMM_TOL = 1e-11
+GEMM_TOL = 2e-11
 LOGDET_TOL = 1e-9
 DIAG_TOL = 1e-8
 
@@ -78,9 +78,10 @@ def test_split_gemm_scaled_rows_and_beta_zero(rgf):
     assert np.max(np.abs(got - ref) / bound) <= GEMM_TOL
 
 
-def test_split_gemm_eight_slices_is_fp64_accurate(rgf):
-    """8 slices (56-bit operands) reach the accuracy of an FP64 GEMM."""
-    out, ref, bound = _gemm_case(rgf, "N", "T", 640, 384, 1500, 1.0, 0.0, seed=3, slices=8)
+@pytest.mark.parametrize("slices", [7, 8])
+def test_split_gemm_seven_slices_is_fp64_accurate(rgf, slices):
+    """7 slices (56-bit operands) reach the accuracy of an FP64 GEMM."""
+    out, ref, bound = _gemm_case(rgf, "N", "T", 640, 384, 1500, 1.0, 0.0, seed=3, slices=slices)
     assert np.max(np.abs(out["split"] - ref) / bound) <= 1e-15
     assert np.max(np.abs(out["split"] - ref) / bound) <= 4 * np.max(np.abs(out["fp64"] - ref) / bound) + 1e-16
 
