@@ -143,7 +143,9 @@ int rgf_get_stream(rgf_handle* h, void** stream);
  * its slicing kernels) *ms receives the summed device time, *launches their
  * number and *flops their algorithmic FP64-equivalent flops since the last
  * reset; kind 3 reports the split GEMMs with *flops = executed bf16
- * slice-product flops.  Stages run without CUDA graphs while it is enabled.
+ * slice-product flops.  While it is enabled stages run without CUDA graphs
+ * and every timed product runs alone (the handle's streams are drained before
+ * it), so the times are those of the kernels themselves.
  * enable = 2 also prints per-shape totals to stderr at each reset. */
 int rgf_kernel_timer_enable(rgf_handle* h, int enable);
 int rgf_kernel_timer_read(rgf_handle* h, int reset, int kind, double* ms, long long* launches,
@@ -202,10 +204,11 @@ int rgf_batch_size(rgf_batch* b, size_t* count);
 /* Instance i as an ordinary handle (solve, export, ... ); owned by the batch. */
 int rgf_batch_handle(rgf_batch* b, size_t i, rgf_handle** h);
 int rgf_batch_get_stream(rgf_batch* b, void** stream);
-/* factorize + logDet + RGFdiag of every instance.  mode 0: one captured CUDA
- * graph with one concurrent branch per instance (built on first use, then
- * replayed with a single launch); mode 1: instance after instance, each with
- * its own stage launches (the per-instance baseline).  logdet[count] and
+/* factorize + logDet + RGFdiag of every instance.  mode 0: all instances at
+ * once, one concurrent branch (stream pair) per instance; the first run
+ * launches the kernels directly, the second captures them into one CUDA graph
+ * that later runs replay with a single launch.  mode 1: instance after
+ * instance, each with its own stage launches (the per-instance baseline).  logdet[count] and
  * diag[i] (n_i doubles; diag or diag[i] may be NULL) receive the results. */
 int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag);
 /* GPU kernels launched by the batch's runs so far. */

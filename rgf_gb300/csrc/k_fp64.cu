@@ -186,11 +186,10 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
 // On GB300 each SM sub-partition has its own FP64 unit; one FP64 warp
 // instruction occupies it ~80 cycles and a dependent FP64 op waits ~64, so the
 // column-to-column pivot chain (next pivot update, its reciprocal square root)
-// is the critical path.  Warp 0 runs that chain alone on sub-partition 0;
-// warps on the other three sub-partitions apply the rank-1 updates from the
-// unscaled column with a per-column factor S[c][j] * y_j^2; all scaling to L
-// happens in one parallel pass at the end; the tile's log-sum uses parallel
-// logs and a fixed-order reduction.
+// is the critical path.  The tile keeps unscaled columns (updates use the
+// factor S[c][j] * y_j^2, y_j = S_jj^{-1/2}); all scaling to L happens in one
+// parallel pass at the end.  The log-determinant is summed later from the
+// factor's diagonal, off this path.
 // ---------------------------------------------------------------------------
 // reciprocal square root of a normal positive double: exponent split with
 // integer ops, an FP32 seed from the top mantissa bits (no FP64 conversion
@@ -216,68 +215,6 @@ __device__ __forceinline__ double rsqrt_fast(double d) {
 }
 
 
-__global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ldt, int nbk,
-                                                         int col0, double* logpart,
-                                                         DevStatus* st) {
-  // warp 0 (sub-partition 0) runs the pivot chain alone; warps 1,2,3,5,6,7
-  // (sub-partitions 1..3) apply the trailing updates; warp 4 shares
-  // sub-partition 0 with warp 0 and stays out of the loop.  S keeps the
-  // unscaled columns; all scaling happens once at the end.
-  __shared__ double S[64][65];
-  __shared__ double ys[64];
-  __shared__ int fail;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const double nan = __longlong_as_double(0x7ff8000000000000LL);
-  for (int c = warp; c < nbk; c += 8)
-    for (int r = c + lane; r < nbk; r += 32) S[r][c] = T[(long long)r + (long long)c * ldt];
-  if (tid == 0) fail = -1;
-  __syncthreads();
-  // trailing-warp index 0..5 for warps 1,2,3,5,6,7
-  const int tw = warp < 4 ? warp - 1 : warp - 2;
-  if (tid == 0) {
-    const double d = S[0][0];
-    if (!(d > 0.0)) fail = 0;
-    ys[0] = d > 0.0 ? rsqrt_fast(d) : nan;
-  }
-  __syncthreads();
-  for (int j = 0; j < nbk; ++j) {
-    const double y = ys[j];
-    if (warp == 0) {
-      if (lane == 0 && j + 1 < nbk) {
-        const double s = S[j + 1][j] * y;
-        const double d = fma(-s, s, S[j + 1][j + 1]);
-        const bool ok = d > 0.0;
-        if (!ok && fail < 0) fail = j + 1;
-        ys[j + 1] = ok ? rsqrt_fast(d) : nan;
-        S[j + 1][j + 1] = d;
-      }
-    } else if (warp != 4) {
-      const double y2 = y * y;
-      for (int c = j + 1 + tw; c < nbk; c += 6) {
-        const double f = S[c][j] * y2;
-        const int r0 = c + lane + (c == j + 1 ? 1 : 0);
-        for (int r = r0; r < nbk; r += 32) S[r][c] = fma(-S[r][j], f, S[r][c]);
-      }
-    }
-    __syncthreads();
-  }
-  // L = S scaled column-wise: L_rj = S_rj * y_j (r > j), L_jj = S_jj * y_j
-  for (int c = warp; c < nbk; c += 8) {
-    const double y = ys[c];
-    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c] * y;
-  }
-  if (warp == 0) {
-    double v = (lane < nbk ? log(S[lane][lane] * ys[lane]) : 0.0) +
-               (lane + 32 < nbk ? log(S[lane + 32][lane + 32] * ys[lane + 32]) : 0.0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) {
-      *logpart = v;
-      if (fail >= 0) atomicMin(&st->not_spd_col, col0 + fail);
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Leaf Cholesky, data-flow form.  Column c of the tile is owned by warp c % 8
 // (two warps per sub-partition, so all four FP64 units work).  Step j applies
@@ -302,8 +239,7 @@ __device__ __forceinline__ int ld_acquire_cta(const int* p) {
 }
 
 __global__ void __launch_bounds__(256) leaf_potrf_flow_kernel(double* T, long long ldt, int nbk,
-                                                              int col0, double* logpart,
-                                                              DevStatus* st) {
+                                                              int col0, DevStatus* st) {
   __shared__ double S[64][65];
   __shared__ double ys[64];
   __shared__ int ready;   // y_0 .. y_ready are published
@@ -363,75 +299,73 @@ __global__ void __launch_bounds__(256) leaf_potrf_flow_kernel(double* T, long lo
     const double y = ys[c];
     for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c] * y;
   }
-  if (warp == 0) {
-    double v = (lane < nbk ? log(S[lane][lane] * ys[lane]) : 0.0) +
-               (lane + 32 < nbk ? log(S[lane + 32][lane + 32] * ys[lane + 32]) : 0.0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) {
-      *logpart = v;
-      if (fail != 0x7fffffff) atomicMin(&st->not_spd_col, col0 + fail);
-    }
-  }
+  if (tid == 0 && fail != 0x7fffffff) atomicMin(&st->not_spd_col, col0 + fail);
 }
 
 // ---------------------------------------------------------------------------
-// Row-parallel triangular solve with a <= 64 x 64 lower tile.  On GB300 each
-// SM sub-partition has its own slow FP64 unit (a dependent DFMA takes ~64
-// cycles; one warp reaches a quarter of the SM's FP64 rate), so a CTA is
-// four warps sharing 32 rows: lane t owns row t (column t of Xs) and warp w
-// applies the updates of the unknowns l = w, w+4, ... after each x_j is
-// final.  Loops stay rolled (a fully unrolled solve stalls on instruction
-// fetch).
+// Row-parallel triangular solve with a <= 64 x 64 lower tile, warp-synchronous.
+// Eight lanes share one row: lane q of the group keeps the unknowns
+// l = q, q + 8, ... in registers.  Step j: the owner of x_j scales it, one
+// shuffle hands it to the other seven lanes, and each applies it to its own
+// unknowns -- no CTA barrier per column, so the column-to-column chain is a
+// multiply, a shuffle and a fused multiply-add.  A warp holds four rows and a
+// CTA of 4 warps 16 rows, so the FP64 work spreads over many SMs (each SM
+// retires only ~3.5 FP64 flops per cycle).
+// MODE 0: x_j = (b_j - sum_{l<j} x_l L_jl) / L_jj   (X L^T = B)
+// MODE 1: x_j = (b_j - sum_{l>j} x_l L_lj) / L_jj   (X L = B)
 // ---------------------------------------------------------------------------
-template <int MODE, int RPB>
+template <int MODE>
 __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs, long long xcs,
                                                          int rows, const double* L, long long ldl,
                                                          int nbk, long long sX, long long sL) {
-  // RPB rows per CTA; the 128 threads are RPB rows x G column groups and
-  // group g applies the updates of the unknowns l = g, g + G, ...
-  constexpr int G = 128 / RPB;
   __shared__ double Ls[64][65];
-  __shared__ double Xs[64][RPB + 1];
   __shared__ double rinv[64];
   X += (long long)blockIdx.y * sX;
   L += (long long)blockIdx.y * sL;
-  const int t = threadIdx.x % RPB, w = threadIdx.x / RPB;
   for (int idx = threadIdx.x; idx < 64 * 64; idx += 128) {
     const int c = idx >> 6, r = idx & 63;
     double v = 0.0;
     if (r < nbk && c < nbk && r >= c) v = L[(long long)r + (long long)c * ldl];
     Ls[r][c] = v;
   }
-  const long long r = (long long)blockIdx.x * RPB + t;
-  const bool live = r < rows;
-  for (int j = w; j < nbk; j += G) Xs[j][t] = live ? X[r * xrs + (long long)j * xcs] : 0.0;
   __syncthreads();
   if (threadIdx.x < 64) rinv[threadIdx.x] = (threadIdx.x < nbk) ? 1.0 / Ls[threadIdx.x][threadIdx.x] : 0.0;
   __syncthreads();
-  if (MODE == 0) {  // x_j = (b_j - sum_{l<j} x_l L_jl) / L_jj
-    for (int j = 0; j < nbk; ++j) {
-      const double xj = Xs[j][t] * rinv[j];
-      __syncthreads();  // every group has read x_j before it is overwritten
-      if (w == 0) Xs[j][t] = xj;
-      // first unknown > j owned by this group
-      const int l0 = j + 1 + ((w - (j + 1)) % G + G) % G;
-#pragma unroll 4
-      for (int l = l0; l < nbk; l += G) Xs[l][t] = fma(-xj, Ls[l][j], Xs[l][t]);
-      __syncthreads();
-    }
-  } else {  // x_j = (b_j - sum_{l>j} x_l L_lj) / L_jj, j descending
-    for (int j = nbk - 1; j >= 0; --j) {
-      const double xj = Xs[j][t] * rinv[j];
-      __syncthreads();
-      if (w == 0) Xs[j][t] = xj;
-#pragma unroll 4
-      for (int l = w; l < j; l += G) Xs[l][t] = fma(-xj, Ls[j][l], Xs[l][t]);
-      __syncthreads();
+  const int lane = threadIdx.x & 31, q = lane & 7, gbase = lane & ~7;
+  const long long r = (long long)blockIdx.x * 16 + (threadIdx.x >> 3);
+  const bool live = r < rows;
+  double u[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const int l = t * 8 + q;
+    u[t] = (live && l < nbk) ? X[r * xrs + (long long)l * xcs] : 0.0;
+  }
+  for (int s = 0; s < nbk; ++s) {
+    const int j = MODE == 0 ? s : nbk - 1 - s;
+    const int jt = j >> 3;
+    double uj = 0.0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (t == jt) uj = u[t];
+    const double xj = __shfl_sync(0xffffffffu, uj * rinv[j], gbase | (j & 7));
+    // slots that can hold a live unknown: a warp-uniform range, so FP64
+    // instructions with no live lane are not issued
+    const int tlo = MODE == 0 ? jt : 0, thi = MODE == 0 ? (nbk - 1) >> 3 : jt;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      if (t < tlo || t > thi) continue;
+      const int l = t * 8 + q;
+      if (l == j) u[t] = xj;
+      if (MODE == 0 ? (l > j && l < nbk) : (l < j)) u[t] = fma(-xj, MODE == 0 ? Ls[l][j] : Ls[j][l], u[t]);
     }
   }
-  if (live)
-    for (int j = w; j < nbk; j += G) X[r * xrs + (long long)j * xcs] = Xs[j][t];
+  if (live) {
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int l = t * 8 + q;
+      if (l < nbk) X[r * xrs + (long long)l * xcs] = u[t];
+    }
+  }
 }
 
 // Thin products (m <= 16, op(B) = B^T): lane = output column, the 4 warps of
@@ -546,41 +480,21 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
   return 1;
 }
 
-void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, double* logpart,
-                       DevStatus* st, cudaStream_t s) {
+void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* st,
+                       cudaStream_t s) {
   if (nbk <= 0) return;
-  static const int variant = [] {
-    const char* e = getenv("RGF_GB300_LEAF_KERNEL");
-    return e ? atoi(e) : 1;
-  }();
-  if (variant == 1)
-    leaf_potrf_flow_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, logpart, st);
-  else
-    leaf_potrf_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, logpart, st);
+  leaf_potrf_flow_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, st);
 }
 
 void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,
                       long long ldl, int nbk, int mode, int batch, long long sX, long long sL,
                       cudaStream_t s) {
   if (rows <= 0 || nbk <= 0 || batch <= 0) return;
-  // Each SM retires only ~3.5 FP64 flops per cycle, so a solve spread over
-  // fewer CTAs than SMs is slow: take fewer rows per CTA when the grid is small.
-  const long long ctas32 = (long long)((rows + 31) / 32) * batch;
-  const int rpb = ctas32 >= 2 * 152 ? 32 : ctas32 * 2 >= 152 ? 16 : 8;
-  dim3 grid((rows + rpb - 1) / rpb, batch);
-#define RGF_TRSM_LAUNCH(R)                                                                   \
-  if (mode == 0)                                                                            \
-    trsm_rows_kernel<0, R><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);    \
-  else                                                                                      \
-    trsm_rows_kernel<1, R><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
-  if (rpb == 32) {
-    RGF_TRSM_LAUNCH(32)
-  } else if (rpb == 16) {
-    RGF_TRSM_LAUNCH(16)
-  } else {
-    RGF_TRSM_LAUNCH(8)
-  }
-#undef RGF_TRSM_LAUNCH
+  dim3 grid((rows + 15) / 16, batch);
+  if (mode == 0)
+    trsm_rows_kernel<0><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+  else
+    trsm_rows_kernel<1><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
 }
 
 }  // namespace rgf

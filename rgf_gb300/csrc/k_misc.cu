@@ -67,6 +67,33 @@ __global__ void ingest_kernel(BtaShape sh, const size_t* __restrict__ ia,
   if (bad) atomicOr(&st->bad_input, 1);
 }
 
+// log of every diagonal entry of the factor MF; each block of 256 columns sums
+// its logs in a fixed tree order into parts[block]
+__global__ void diag_log_kernel(BtaShape sh, const double* MF, double* parts) {
+  __shared__ double v[256];
+  const long long k = (long long)blockIdx.x * 256 + threadIdx.x;
+  double x = 0.0;
+  if (k < sh.n) {
+    const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
+    long long pos;
+    if (k < ns * nt) {
+      const long long i = k / ns, j = k - i * ns;
+      pos = col_offset_d(ns, nt, nd, i) + j * (lda_d(ns, nt, nd, i) + 1);
+    } else {
+      const long long j = k - ns * nt;
+      pos = col_offset_d(ns, nt, nd, nt) + j * (nd + 1);
+    }
+    x = log(MF[pos]);
+  }
+  v[threadIdx.x] = x;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) v[threadIdx.x] += v[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) parts[blockIdx.x] = v[0];
+}
+
 __global__ void logdet_reduce_kernel(const double* parts, int nparts, double* out) {
   const int lane = threadIdx.x;
   double s = 0.0;
@@ -201,8 +228,13 @@ void launch_ingest(const BtaShape& sh, const size_t* ia, const size_t* ja, const
   ingest_kernel<<<(unsigned)((threads + bs - 1) / bs), bs, 0, s>>>(sh, ia, ja, a, MF, st);
 }
 
-void launch_logdet_reduce(const double* parts, int nparts, double* out, cudaStream_t s) {
-  logdet_reduce_kernel<<<1, 32, 0, s>>>(parts, nparts, out);
+int logdet_parts(const BtaShape& sh) { return (int)((sh.n + 255) / 256); }
+
+void launch_logdet(const BtaShape& sh, const double* MF, double* parts, double* out,
+                   cudaStream_t s) {
+  const int np = logdet_parts(sh);
+  diag_log_kernel<<<np, 256, 0, s>>>(sh, MF, parts);
+  logdet_reduce_kernel<<<1, 32, 0, s>>>(parts, np, out);
 }
 
 void launch_extract_diag(const BtaShape& sh, const double* MS, double* diag, cudaStream_t s) {

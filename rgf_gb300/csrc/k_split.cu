@@ -529,10 +529,13 @@ __global__ void slice_kernel(const double* X, long long rs, long long ks, int R,
 }
 
 // Both operands of a product with a short K in one launch: a CTA owns 32 rows
-// of op(A) or op(B) (blockIdx.x below nblkA: A), finds their maximum
-// magnitudes over all of K, then writes the S digit planes tile by tile.
+// of op(A) or op(B) (blockIdx.x below nblkA: A) and SLICE_KC terms of K
+// (blockIdx.y); it finds the rows' maximum magnitudes over all of K, then
+// writes the S digit planes of its K range tile by tile.
 // Replaces the max / exponent / slice kernels (and the memsets) of the long-K
 // path, which dominate small products.
+constexpr int SLICE_KC = 128;  // K terms sliced per CTA of slice_pair_kernel
+
 struct SliceOperand {
   const double* X;
   const double* X2;  // rows >= R1 from X2 + (r - R1) (rs == 1 only), or nullptr
@@ -562,7 +565,8 @@ __global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOp
   // pass 1: row maxima of |x| as bit patterns
   if (o.rs == 1) {  // rows contiguous: lane = row, warp = k phase
     unsigned long long m = 0;
-    for (int k = ty; k < K; k += 8) {
+#pragma unroll 8
+    for (int k = ty; k < K; k += 8) {  // independent loads in flight
       const unsigned long long v =
           (unsigned long long)__double_as_longlong(val(r0 + tx, k)) & 0x7fffffffffffffffull;
       m = v > m ? v : m;
@@ -573,6 +577,7 @@ __global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOp
     for (int i = 0; i < 4; ++i) {
       const int rl = ty + 8 * i;
       unsigned long long m = 0;
+#pragma unroll 4
       for (int k = tx; k < K; k += 32) {
         const unsigned long long v =
             (unsigned long long)__double_as_longlong(val(r0 + rl, k)) & 0x7fffffffffffffffull;
@@ -595,13 +600,15 @@ __global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOp
     const int r = r0 + threadIdx.x;
     const int e = r < o.R ? exp_of_max(m) : 0;
     exs[threadIdx.x] = e;
-    if (r < o.Rp) ex[r] = e;
+    if (r < o.Rp && blockIdx.y == 0) ex[r] = e;
   }
   __syncthreads();
   // pass 2: digits, one 32 x 32 tile at a time (read along the contiguous
   // dimension, write along k)
   const size_t plane = (size_t)o.Rp * Kp;
-  for (int k0 = 0; k0 < Kp; k0 += 32) {
+  // this CTA's K range: SLICE_KC terms (blockIdx.y); the row maxima above span all of K
+  const int kend = min(Kp, ((int)blockIdx.y + 1) * SLICE_KC);
+  for (int k0 = blockIdx.y * SLICE_KC; k0 < kend; k0 += 32) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       int rl, kl;
@@ -824,8 +831,8 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       SliceOperand ob{B, nullptr, g.transB ? 1 : g.ldb, g.transB ? g.ldb : 1, g.sB, g.n, g.n,
                       RpB, triBt, exB, sb};
       const int nblkA = RpA / 32, nblkB = same ? 0 : RpB / 32;
-      slice_pair_kernel<<<dim3(nblkA + nblkB, 1, nbat), 256, 0, s>>>(oa, ob, nblkA, g.k, Kp, S,
-                                                                     beta);
+      slice_pair_kernel<<<dim3(nblkA + nblkB, (Kp + SLICE_KC - 1) / SLICE_KC, nbat), 256, 0, s>>>(
+          oa, ob, nblkA, g.k, Kp, S, beta);
       launched += 1;
     } else {
       if (!g.transA) slice(A, 1, g.lda, g.sA, g.m, g.triA, exA, mxA, sa, RpA, A2, g.mA1);

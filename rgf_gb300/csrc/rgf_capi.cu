@@ -176,6 +176,10 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
       e1 = h->ev_pool.back().second;
       h->ev_pool.pop_back();
     }
+    // each timed product runs alone: both streams drained before it starts,
+    // so its events measure the kernels themselves, not queueing or overlap
+    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->side);
     cudaEventRecord(e0, cur_stream(h));
   }
   long long launched = 1;
@@ -183,19 +187,24 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   SplitEngine* eng = h->on_side ? h->split_side : h->split;
   bool split = eng && may_split && eng->supports(g);
   if (split) {
-    // Route by estimated time.  A split product has a fixed cost of a few
-    // small slicing kernels and tensor tiles padded to 128 x 128; the FP64
-    // DMMA kernel (split-K for small grids) has almost none but runs at
-    // ~1 TFLOP/s.  Small or thin products are faster in FP64 (which is also
-    // FP64-accurate).
+    // Route by estimated time (fitted to per-shape timings on GB300).  A split
+    // product costs ~50 us of pipeline start-up and drains, its slicing
+    // (~10 us for K <= 512, ~25 us above, plus operand traffic), and per
+    // 148-tile wave ~100 ns per 128x128x16 slice MMA; the FP64 DMMA kernel
+    // costs ~9 us of launches and runs at ~0.9 TFLOP/s.  Small or thin
+    // products are faster in FP64 (which is also FP64-accurate).
     const int S = slices > 0 ? slices : eng->slices();
     const double pairs = S * (S + 1) / 2.0;
     auto up = [](double x, double m) { return std::ceil(x / m) * m; };
-    // short K: both operands sliced in one launch
-    const double fixed = up(g.k, 64) <= 512 ? 15e-6 : (g.A == g.B ? 40e-6 : 70e-6);
-    const double t_split = fixed + pairs * 2.0 * up(g.m, 128) * up(g.n, 128) * up(g.k, 128) *
-                                       g.batch / 700e12;
-    const double t_fp64 = 8e-6 + gemm_flops(g) / 0.8e12;
+    const double kq = up(g.k, 128);
+    double tiles = up(g.m, 128) / 128.0 * (up(g.n, 128) / 128.0) * g.batch;
+    if (g.outLower && g.m == g.n) tiles = tiles * 0.5 + up(g.m, 128) / 256.0 * g.batch;
+    const double waves = std::ceil(tiles / 148.0);
+    const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB;
+    const double t_slice = (kq <= 512 ? 10e-6 : 25e-6) +
+                           (g.m + (same ? 0.0 : g.n)) * kq * 8.0 * g.batch / 3e12;
+    const double t_split = 50e-6 + t_slice + waves * pairs * (kq / 16.0) * 100e-9;
+    const double t_fp64 = 9e-6 + gemm_flops(g) / 0.9e12;
     split = t_split < t_fp64;
   }
   if (split) {
@@ -213,8 +222,8 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   }
 }
 
-void leaf_potrf(rgf_handle* h, double* T, long long ldt, int nbk, int col0, double* part) {
-  launch_leaf_potrf(T, ldt, nbk, col0, part, h->d_status, cur_stream(h));
+void leaf_potrf(rgf_handle* h, double* T, long long ldt, int nbk, int col0) {
+  launch_leaf_potrf(T, ldt, nbk, col0, h->d_status, cur_stream(h));
   h->kernels_issued++;
 }
 
@@ -239,13 +248,12 @@ void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
 // nothing on that path reads.  With look-ahead on, their solves and updates
 // go to the side stream, ordered after the main-stream work they read, so the
 // critical path only carries the diagonal block.
-void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int dr, int col0,
-                 int part0) {
+void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, int dr, int col0) {
   const int nb = h->nb;
   const bool la = h->lookahead && h->side;
   const int split_row = la ? dr : rows;  // rows at or past this go to the side stream
   if (cols <= nb) {
-    leaf_potrf(h, P, lda, cols, col0, h->d_logpart + part0);
+    leaf_potrf(h, P, lda, cols, col0);
     if (split_row > cols) trsm_rows(h, P + cols, 1, lda, split_row - cols, P, lda, cols, 0);
     if (rows > split_row) {
       fork_side(h);
@@ -256,7 +264,7 @@ void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, in
     return;
   }
   const int c1 = ((cols / 2 + nb - 1) / nb) * nb;
-  panel_potrf(h, P, lda, rows, c1, dr, col0, part0);
+  panel_potrf(h, P, lda, rows, c1, dr, col0);
   // trailing update: P[c1:rows, c1:cols] -= P[c1:rows, 0:c1] P[c1:cols, 0:c1]^T
   auto upd = [&](int r0, int m, int cls) {
     if (m <= 0) return;
@@ -283,8 +291,7 @@ void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, in
   } else {
     upd(c1, split_row - c1, BULK);
   }
-  panel_potrf(h, P + c1 + (long long)c1 * lda, lda, rows - c1, cols - c1, dr - c1, col0 + c1,
-              part0 + c1 / nb);
+  panel_potrf(h, P + c1 + (long long)c1 * lda, lda, rows - c1, cols - c1, dr - c1, col0 + c1);
 }
 
 // ---- stage 1: factorize (RGF.H:233-340) ----
@@ -297,7 +304,6 @@ void issue_factor(rgf_handle* h) {
   launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, s);
   h->kernels_issued += 2;
   double* corner = h->d_MF + mf_col_offset(sh, nt);
-  const int tiles = (int)((ns + h->nb - 1) / h->nb);
   for (long long i = 0; i < nt; ++i) {
     double* P = h->d_MF + mf_col_offset(sh, i);
     const long long lda = mf_lda(sh, i);
@@ -327,7 +333,7 @@ void issue_factor(rgf_handle* h) {
         gemm(h, c, SMALL);
       }
     }
-    panel_potrf(h, P, lda, (int)lda, (int)ns, (int)ns, (int)(i * ns), (int)(i * tiles));
+    panel_potrf(h, P, lda, (int)lda, (int)ns, (int)ns, (int)(i * ns));
     if (h->lookahead && h->side && lda > ns) join_side(h);
   }
   if (nd > 0) {
@@ -339,11 +345,10 @@ void issue_factor(rgf_handle* h) {
     c.C = c.D = corner; c.ldc = c.ldd = nd;
     c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
     gemm(h, c, SMALL);
-    panel_potrf(h, corner, nd, (int)nd, (int)nd, (int)nd, (int)(nt * ns),
-                (int)(nt * tiles));  // RGF.H:335
+    panel_potrf(h, corner, nd, (int)nd, (int)nd, (int)nd, (int)(nt * ns));  // RGF.H:335
   }
-  launch_logdet_reduce(h->d_logpart, h->nparts, h->d_scalars, s);
-  h->kernels_issued++;
+  launch_logdet(sh, h->d_MF, h->d_logpart, h->d_scalars, s);
+  h->kernels_issued += 2;
 }
 
 // For every diagonal block at once: U_i = L_ii^{-T} (upper triangular).
@@ -591,7 +596,8 @@ void issue_solve(rgf_handle* h, int nrhs) {
 // The first run of a stage launches its kernels directly; from the second run
 // on, the stage is captured once into a CUDA graph and replayed.  A handle
 // used once (create, factorize, RGFdiag, destroy) never pays for a capture
-// and instantiation of tens of thousands of nodes.
+// and instantiation of tens of thousands of nodes.  With the kernel timer on
+// the stage runs launch by launch.
 template <class F>
 int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, int* runs, F issue) {
   if (h->timer_on || !h->opts.use_graphs || (!*exec && (*runs)++ == 0)) {
@@ -816,8 +822,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
       const int v = std::atoi(e);
       if (v == 16 || v == 32 || v == 64) h->nb = v;
     }
-    const int tiles = (int)((ns + h->nb - 1) / h->nb), dtiles = (int)((nd + h->nb - 1) / h->nb);
-    h->nparts = (int)(nt * tiles + dtiles);
+    h->nparts = logdet_parts(h->sh);
     if ((st = dalloc(h, &h->d_logpart, h->nparts))) break;
     if ((st = dalloc(h, &h->d_scalars, 8))) break;
     if ((st = dalloc(h, &h->d_diag, n))) break;
@@ -1105,6 +1110,7 @@ struct rgf_batch {
   cudaGraphExec_t g_all = nullptr;
   long long k_all = 0;
   long long kernels_total = 0;
+  int runs = 0;  // graph-mode runs so far (the first one is not captured)
 };
 
 namespace {
@@ -1120,7 +1126,12 @@ void batch_release(rgf_batch* b) {
   delete b;
 }
 
-int batch_build_graph(rgf_batch* b) {
+// Every instance's factorize + selected inversion, each on its own streams,
+// forked from and joined back into the batch stream.  capture = true records
+// it as one CUDA graph (b->g_all); otherwise the kernels are launched directly
+// (the first run: a batch used once never pays for capturing and
+// instantiating a graph of hundreds of thousands of nodes).
+int batch_issue(rgf_batch* b, bool capture) {
   for (rgf_handle* h : b->h) {
     int st = alloc_selinv(h);
     if (st) return st;
@@ -1133,7 +1144,7 @@ int batch_build_graph(rgf_batch* b) {
     for (auto& e : b->ev) RGF_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   cudaGraph_t graph = nullptr;
-  RGF_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  if (capture) RGF_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   cudaEventRecord(b->ev[0], b->stream);
   long long nk = 0;
   for (size_t i = 0; i < n; ++i) {
@@ -1145,6 +1156,11 @@ int batch_build_graph(rgf_batch* b) {
     nk += h->kernels_issued;
     cudaEventRecord(b->ev[i + 1], h->stream);
     cudaStreamWaitEvent(b->stream, b->ev[i + 1], 0);
+  }
+  if (!capture) {
+    b->kernels_total += nk;
+    RGF_CK(cudaGetLastError());
+    return RGF_OK;
   }
   cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
   if (e != cudaSuccess) return cuda_status(e);
@@ -1217,10 +1233,14 @@ int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag) {
   if (cudaSetDevice(b->device) != cudaSuccess) return RGF_ECUDA;
   int st = RGF_OK;
   if (mode == 0) {
-    if (!b->g_all && (st = batch_build_graph(b))) return st;
-    RGF_CK(cudaGraphLaunch(b->g_all, b->stream));
+    if (b->runs++ == 0) {
+      if ((st = batch_issue(b, false))) return st;
+    } else {
+      if (!b->g_all && (st = batch_issue(b, true))) return st;
+      RGF_CK(cudaGraphLaunch(b->g_all, b->stream));
+      b->kernels_total += b->k_all;
+    }
     RGF_CK(cudaStreamSynchronize(b->stream));
-    b->kernels_total += b->k_all;
     for (rgf_handle* h : b->h) {
       h->factored = false;
       h->selinv_done = false;

@@ -56,10 +56,9 @@ double gemm_flops(const GemmDesc& g);
 int launch_gemm_fp64(const GemmDesc& g, cudaStream_t s);
 
 // Cholesky of the nbk x nbk (nbk <= 64) lower tile at T (column-major, ldt),
-// in place.  Writes sum(log diag) of the tile to *logpart and records the
-// first non-positive pivot (global column col0 + j) in st.
-void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, double* logpart,
-                       DevStatus* st, cudaStream_t s);
+// in place.  Records the first non-positive pivot (global column col0 + j) in st.
+void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* st,
+                       cudaStream_t s);
 
 // Row-parallel triangular solve with an nbk x nbk (nbk <= 64) lower tile L:
 //   mode 0: X := X * L^{-T}   (forward,  "R L T N")
@@ -85,7 +84,11 @@ long long mf_dense_row(const BtaShape& sh, long long i);
 void launch_ingest(const BtaShape& sh, const size_t* ia, const size_t* ja, const double* a,
                    double* MF, DevStatus* st, cudaStream_t s);
 // Sum of nparts partial log sums, times 2, in a fixed order -> *out.
-void launch_logdet_reduce(const double* parts, int nparts, double* out, cudaStream_t s);
+// *out = 2 sum(log diag(L)) over the factor MF: per-block sums into parts
+// (logdet_parts(sh) of them), then a fixed-order total.
+int logdet_parts(const BtaShape& sh);
+void launch_logdet(const BtaShape& sh, const double* MF, double* parts, double* out,
+                   cudaStream_t s);
 // diag[k] = MS[diag position of k] for all k < n.
 void launch_extract_diag(const BtaShape& sh, const double* MS, double* diag, cudaStream_t s);
 // batch of identity matrices (m x m, ld) at X + b*stride
