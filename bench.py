@@ -492,6 +492,22 @@ def run_rgf(args, w):
     h2d = ia_p.nbytes + ja_p.nbytes + a_p.nbytes
     d2h = diag_host.nbytes + 8
 
+    # 8-RHS solve on the resident factor (refined in FP64 in split precision):
+    # time per call (host arrays in and out) and the worst normalized residual
+    solve_info = None
+    if not args.no_solve:
+        from rgf_gb300 import gen as _gen
+        bsol = _gen.random_rhs(n, 8, w["seed"])
+        xsol = np.empty_like(bsol)
+        s.solve(xsol, bsol, 8)
+        t0 = time.perf_counter()
+        s.solve(xsol, bsol, 8)
+        sms = (time.perf_counter() - t0) * 1e3
+        res = max(s.residualNormNormalized(np.ascontiguousarray(xsol[:, q]),
+                                           np.ascontiguousarray(bsol[:, q])) for q in range(8))
+        solve_info = {"nrhs": 8, "ms": sms, "max_residual_normalized": res,
+                      "refined": args.precision == "split"}
+
     # roofline of the dominant kernel class (timed live over the timed region)
     peak64 = rgf_gb300.measure_fp64_peak()
     peaks, src = load_peaks()
@@ -565,7 +581,7 @@ def run_rgf(args, w):
                          "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "parts": e2e_parts} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
-                "plain_fp64": plain,
+                "plain_fp64": plain, "solve": solve_info,
                 "clocks": clk, "logdet": logdet,
                 "timed_region": "each stage replayed as one CUDA graph; kernel classes timed "
                                 "on one extra step with events around every GEMM, each run "
@@ -589,6 +605,7 @@ def main():
     p.add_argument("--serve-requests", type=int, default=400)
     p.add_argument("--serve-pool", type=int, default=24)
     p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--no-solve", action="store_true", help="skip the 8-RHS solve measurement")
     p.add_argument("--serve-warm", type=int, default=8,
                    help="factors made resident before the request stream starts")
     p.add_argument("--serve-budget-gb", type=float, default=160.0)

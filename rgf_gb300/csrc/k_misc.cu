@@ -262,6 +262,32 @@ void launch_zero_upper(double* X, long long ld, int m, int batch, long long stri
   zero_upper_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ld, m, stride);
 }
 
+// r = b - y; x += d (element-wise over len entries)
+__global__ void sub_kernel(long long len, const double* b, const double* y, double* r) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < len) r[i] = b[i] - y[i];
+}
+__global__ void add_kernel(long long len, double* x, const double* d) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < len) x[i] += d[i];
+}
+
+void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size_t* ja,
+                             const double* a, const double* X, const double* B, double* Y,
+                             double* R, cudaStream_t s) {
+  cudaMemsetAsync(Y, 0, sizeof(double) * n * nrhs, s);
+  const long long threads = n * 32;
+  for (int q = 0; q < nrhs; ++q)
+    sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, X + q * n,
+                                                                      Y + q * n);
+  const long long len = n * nrhs;
+  sub_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, B, Y, R);
+}
+
+void launch_add(long long len, double* x, const double* d, cudaStream_t s) {
+  add_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, x, d);
+}
+
 void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
                      const double* x, const double* b, double* scratch, double* out,
                      cudaStream_t s) {

@@ -27,6 +27,7 @@ using namespace rgf;
 
 namespace {
 constexpr int NB = 64;  // leaf tile of the FP64 panel Cholesky / triangular solves
+constexpr int RGF_REFINE_STEPS = 2;  // FP64 refinement steps of a split-precision solve
 }
 
 struct rgf_handle {
@@ -61,6 +62,8 @@ struct rgf_handle {
   double* d_partial = nullptr;  // arrowhead partial sums, nt * nrhs * nd
   size_t partial_cap = 0;
   double* d_res = nullptr;      // residual scratch: x, b, y (3n)
+  double* d_ref = nullptr;      // refinement of split solves: x, b, y (3 n nrhs)
+  size_t ref_cap = 0;           // doubles
   double* d_gemm_ws = nullptr;  // split-K partial sums of small FP64 GEMMs
   double* d_gemm_ws_side = nullptr;  // the same for the side stream
   long long gemm_ws_elems = 0;
@@ -724,7 +727,7 @@ void release(rgf_handle* h) {
   delete h->split_side;
   void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
                   h->d_logpart, h->d_scalars, h->d_diag, h->d_status, h->d_rhs, h->d_partial,
-                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side};
+                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side, h->d_ref};
   for (void* p : bufs) dfree(p);
   if (h->side) cudaStreamSynchronize(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -931,14 +934,45 @@ int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
     if ((st = dalloc(h, &h->d_partial, pneed))) return st;
     h->partial_cap = pneed;
   }
+  // Split precision: the factor is accurate to ~1e-10, so the solve is
+  // refined in FP64 (RGF_REFINE_STEPS times): r = b - A x from the resident
+  // CSC, x += A~^{-1} r with the same factor.
+  const bool refine = h->opts.precision == RGF_PREC_SPLIT;
+  if (refine && need * 3 > h->ref_cap) {
+    dfree(h->d_ref);
+    h->device_bytes -= h->ref_cap * sizeof(double);
+    h->ref_cap = 0;
+    if ((st = dalloc(h, &h->d_ref, need * 3))) return st;
+    h->ref_cap = need * 3;
+  }
+  double* xr = h->d_ref;
+  double* br = refine ? h->d_ref + need : nullptr;
+  double* yr = refine ? h->d_ref + 2 * need : nullptr;
   RGF_CK(cudaMemcpyAsync(h->d_rhs, b, sizeof(double) * need, cudaMemcpyHostToDevice, h->stream));
+  if (refine)
+    RGF_CK(cudaMemcpyAsync(br, h->d_rhs, sizeof(double) * need, cudaMemcpyDeviceToDevice,
+                           h->stream));
   auto it = h->g_solve.find(nrhs);
   cudaGraphExec_t exec = it == h->g_solve.end() ? nullptr : it->second.first;
   long long nk = it == h->g_solve.end() ? 0 : it->second.second;
-  st = run_stage(h, &exec, &nk, &h->runs_solve[nrhs], [&] { issue_solve(h, (int)nrhs); });
-  if (st) return st;
-  if (exec) h->g_solve[nrhs] = {exec, nk};
-  RGF_CK(cudaMemcpyAsync(x, h->d_rhs, sizeof(double) * need, cudaMemcpyDeviceToHost, h->stream));
+  const int passes = refine ? 1 + RGF_REFINE_STEPS : 1;
+  for (int pass = 0; pass < passes; ++pass) {
+    if (pass > 0)  // d_rhs = b - A x
+      launch_residual_vectors(n, (int)nrhs, h->d_ia, h->d_ja, h->d_a, xr, br, yr, h->d_rhs,
+                              h->stream);
+    st = run_stage(h, &exec, &nk, &h->runs_solve[nrhs], [&] { issue_solve(h, (int)nrhs); });
+    if (st) return st;
+    if (exec) h->g_solve[nrhs] = {exec, nk};
+    if (refine) {
+      if (pass == 0)
+        RGF_CK(cudaMemcpyAsync(xr, h->d_rhs, sizeof(double) * need, cudaMemcpyDeviceToDevice,
+                               h->stream));
+      else
+        launch_add((long long)need, xr, h->d_rhs, h->stream);
+    }
+  }
+  RGF_CK(cudaMemcpyAsync(x, refine ? xr : h->d_rhs, sizeof(double) * need,
+                         cudaMemcpyDeviceToHost, h->stream));
   return sync_and_check(h);
 }
 

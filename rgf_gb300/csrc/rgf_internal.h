@@ -105,6 +105,12 @@ void launch_zero_upper(double* X, long long ld, int m, int batch, long long stri
 void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
                      const double* x, const double* b, double* scratch, double* out,
                      cudaStream_t s);
+// R = B - A X for nrhs columns (ld n) from the lower CSC; Y is n*nrhs scratch
+void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size_t* ja,
+                             const double* a, const double* X, const double* B, double* Y,
+                             double* R, cudaStream_t s);
+// x += d over len entries
+void launch_add(long long len, double* x, const double* d, cudaStream_t s);
 // out[q*ldo + dd] = sum_i sum_j C_i(dd, j) * R_i(j, q) over block columns,
 // computed as per-block partials then an ordered sum: the arrowhead part of
 // the forward solve.  y_d -= that.

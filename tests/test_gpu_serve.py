@@ -3,7 +3,8 @@
 Factorizations, solves and RGFdiag requests on several resident factors are
 submitted together so that they overlap on the GPU; every result must be
 bitwise what a fresh instance computes alone (the kernels are deterministic
-and independent of what else runs).  Eviction: a budget that holds one
+and independent of what else runs) -- except split-precision solves, whose
+FP64 refinement residual sums with atomics: those agree to 1e-13 relative.  Eviction: a budget that holds one
 factor evicts the older one, and a request for it fails cleanly.
 """
 import numpy as np
@@ -41,7 +42,10 @@ def test_results_in_the_mix_equal_alone(rgf, precision):
         alone = rgf.RGF(*mats[i], ns, nt, nd, precision=precision)
         if kind == "solve":
             x = alone.solve(np.empty_like(b, order="F"), b, b.shape[1])
-            assert np.array_equal(r["x"], x)
+            if precision == "fp64":
+                assert np.array_equal(r["x"], x)
+            else:
+                assert np.max(np.abs(r["x"] - x)) <= 1e-13 * np.max(np.abs(x))
         elif kind == "diag":
             assert np.array_equal(r["diag"], alone.RGFdiag())
         else:
