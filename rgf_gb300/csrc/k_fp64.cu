@@ -402,6 +402,58 @@ __global__ void __launch_bounds__(128) gemm_thin_m_kernel(GemmDesc g, int kchunk
   }
 }
 
+// Thin products (n <= 16, op(B) = B): thread = output row; the CTA's 128 rows
+// share 32-term K tiles of op(A) and op(B) staged through shared memory (read
+// along A's contiguous dimension either way), so every FP64 instruction has
+// all lanes busy.  blockIdx.y selects a K chunk; partial sums go to the
+// split-K workspace in the GEMM kernel's layout.  op(A) may be triangular.
+__global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk) {
+  __shared__ double As[32][129];
+  __shared__ double Bs[32][17];
+  const int tid = threadIdx.x;
+  const int r0 = blockIdx.x * 128, r = r0 + tid;
+  int k0 = blockIdx.y * kchunk, k1 = min(g.k, k0 + kchunk);
+  if (g.triA == TRI_LOWER) k1 = min(k1, r0 + 128);  // op(A)(r, kk) = 0 for kk > r
+  if (g.triA == TRI_UPPER) k0 = max(k0, r0);        // op(A)(r, kk) = 0 for kk < r
+  double acc[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) acc[c] = 0.0;
+  for (int kt = k0; kt < k1; kt += 32) {
+    for (int idx = tid; idx < 32 * 128; idx += 128) {
+      int i, kk;
+      if (!g.transA) { i = idx & 127; kk = idx >> 7; }
+      else           { kk = idx & 31; i = idx >> 5; }
+      const int row = r0 + i, kg = kt + kk;
+      bool ok = row < g.m && kg < k1;
+      if (g.triA == TRI_LOWER) ok = ok && kg <= row;
+      if (g.triA == TRI_UPPER) ok = ok && kg >= row;
+      double v = 0.0;
+      if (ok) v = g.transA ? g.A[(long long)kg + (long long)row * g.lda]
+                           : g.A[(long long)row + (long long)kg * g.lda];
+      As[kk][i] = v;
+    }
+    for (int idx = tid; idx < 32 * 16; idx += 128) {
+      const int kk = idx & 31, c = idx >> 5, kg = kt + kk;
+      Bs[kk][c] = (c < g.n && kg < k1) ? g.B[(long long)kg + (long long)c * g.ldb] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < 32; ++kk) {
+      const double a = As[kk][tid];
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c < g.n) acc[c] = fma(a, Bs[kk][c], acc[c]);
+    }
+    __syncthreads();
+  }
+  if (r < g.m) {
+    double* W = g.ws + (long long)blockIdx.y * g.m * g.n;
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      if (c < g.n) W[(long long)r + (long long)c * g.m] = acc[c];
+  }
+}
+
 // D = alpha * sum_s W_s + beta * C over the split-K partials, in slice order.
 __global__ void splitk_reduce_kernel(GemmDesc g) {
   const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
@@ -439,6 +491,21 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
       const int kchunk = (g.k + kchunks - 1) / kchunks;
       g.ksplit = kchunks;
       gemm_thin_m_kernel<<<dim3(cx, kchunks), 128, 0, s>>>(g, kchunk);
+      dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
+      splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
+      return 2;
+    }
+  }
+  if (g.n <= 16 && !g.transB && g.triB == TRI_NONE && g.batch == 1 && g.ws && !g.outLower &&
+      !g.A2) {
+    const int rb = (g.m + 127) / 128;
+    int kchunks = std::max(1, std::min((2 * 152 + rb - 1) / rb, (g.k + 31) / 32));
+    while (kchunks > 1 && (long long)kchunks * g.m * g.n > g.ws_elems) --kchunks;
+    if ((long long)kchunks * g.m * g.n <= g.ws_elems) {
+      const int kchunk = ((g.k + kchunks - 1) / kchunks + 31) / 32 * 32;
+      kchunks = (g.k + kchunk - 1) / kchunk;
+      g.ksplit = kchunks;
+      gemm_thin_n_kernel<<<dim3(rb, kchunks), 128, 0, s>>>(g, kchunk);
       dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
       splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
       return 2;

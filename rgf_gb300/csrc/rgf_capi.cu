@@ -58,6 +58,7 @@ struct rgf_handle {
   double* d_diag = nullptr;
   DevStatus* d_status = nullptr;
   double* d_rhs = nullptr;
+  double* d_rhs2 = nullptr;  // y of the block substitution (rhs_cap doubles)
   size_t rhs_cap = 0;           // doubles
   double* d_partial = nullptr;  // arrowhead partial sums, nt * nrhs * nd
   size_t partial_cap = 0;
@@ -70,13 +71,14 @@ struct rgf_handle {
 
   bool factored = false;
   bool selinv_done = false;
+  bool inv_done = false;  // U holds the inverses of the current factor's blocks
   int not_spd_col = -1;
   size_t device_bytes = 0;
 
-  cudaGraphExec_t g_factor = nullptr, g_selinv = nullptr;
-  long long k_factor = 0, k_selinv = 0;
+  cudaGraphExec_t g_factor = nullptr, g_selinv = nullptr, g_inv = nullptr;
+  long long k_factor = 0, k_selinv = 0, k_inv = 0;
   std::map<size_t, std::pair<cudaGraphExec_t, long long>> g_solve;
-  int runs_factor = 0, runs_selinv = 0;  // stage runs so far (the first one is not captured)
+  int runs_factor = 0, runs_selinv = 0, runs_inv = 0;  // stage runs so far (the first is not captured)
   std::map<size_t, int> runs_solve;
   long long kernels_issued = 0;   // kernels of the stage being recorded
   long long kernels_total = 0;    // kernels launched over the handle's life
@@ -410,6 +412,27 @@ GemmDesc mk(int m, int n, int k, const double* A, long long lda, int tA, const d
   return g;
 }
 
+// U_i = L_ii^{-T} of every diagonal block and of the corner, as one batched
+// recursive TRTRI (the blocks are independent once the factor exists); MS is
+// the recursion's scratch.
+void issue_inverses(rgf_handle* h) {
+  const BtaShape& sh = h->sh;
+  const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
+  const long long ss = ns * ns;
+  // The inverses are upper triangular and are read as full blocks
+  // (W^T = U_i - ...); the recursion writes only their upper part, so the
+  // strictly lower part must be zero.
+  cudaMemsetAsync(h->d_U, 0, sizeof(double) * (nt * ss + nd * nd), h->stream);
+  if (nt > 1)
+    issue_trtri(h, h->d_U, ns, ns, h->d_MF, 2 * ns + nd, h->d_MS, 2 * ns + nd, (int)(nt - 1), ss,
+                ns * (2 * ns + nd), ns * (2 * ns + nd));
+  issue_trtri(h, h->d_U + (nt - 1) * ss, ns, ns, h->d_MF + mf_col_offset(sh, nt - 1), ns + nd,
+              h->d_MS + mf_col_offset(sh, nt - 1), ns + nd, 1, 0, 0, 0);
+  if (nd > 0)
+    issue_trtri(h, h->d_U + nt * ss, nd, nd, h->d_MF + mf_col_offset(sh, nt), nd,
+                h->d_MS + mf_col_offset(sh, nt), nd, 1, 0, 0, 0);
+}
+
 // ---- stage 3: selected inversion ----
 void issue_selinv(rgf_handle* h) {
   const BtaShape& sh = h->sh;
@@ -419,18 +442,8 @@ void issue_selinv(rgf_handle* h) {
   const long long ss = ns * ns;
   double* Ud = h->d_U + nt * ss;
   double* Sdd = h->d_MS + mf_col_offset(sh, nt);
-  // The inverses are upper triangular and are read below as full blocks
-  // (W^T = U_i - ...); the recursion writes only their upper part, so the
-  // strictly lower part must be zero.
-  cudaMemsetAsync(h->d_U, 0, sizeof(double) * (nt * ss + nd * nd), s);
-  // batched inverses of all diagonal blocks
-  if (nt > 1)
-    issue_trtri(h, h->d_U, ns, ns, h->d_MF, 2 * ns + nd, h->d_MS, 2 * ns + nd, (int)(nt - 1), ss,
-                ns * (2 * ns + nd), ns * (2 * ns + nd));
-  issue_trtri(h, h->d_U + (nt - 1) * ss, ns, ns, h->d_MF + mf_col_offset(sh, nt - 1), ns + nd,
-              h->d_MS + mf_col_offset(sh, nt - 1), ns + nd, 1, 0, 0, 0);
+  issue_inverses(h);
   if (nd > 0) {
-    issue_trtri(h, Ud, nd, nd, h->d_MF + mf_col_offset(sh, nt), nd, Sdd, nd, 1, 0, 0, 0);
     // Sigma_dd = L_dd^{-T} L_dd^{-1} = U_d U_d^T   (RGF.H:439-442)
     gemm(h, mk(ind, ind, ind, Ud, nd, 0, Ud, nd, 1, nullptr, 0, Sdd, nd, 1.0, 0.0), SMALL);
   }
@@ -551,47 +564,58 @@ void trsv_lower_t(rgf_handle* h, const double* L, long long ldl, int m, double* 
 }
 
 // ---- stage 2: solve (RGF.H:344-418) on the device buffer d_rhs ----
+// Block substitution with the inverted diagonal blocks U_i = L_ii^{-T}: every
+// step is a product (FP64, spread over the GPU by split K) instead of a chain
+// of small triangular solves.  y lives in d_rhs2, b and then x in d_rhs.
 void issue_solve(rgf_handle* h, int nrhs) {
   const BtaShape& sh = h->sh;
   const long long ns = sh.ns, nt = sh.nt, nd = sh.nd, n = sh.n;
   const int ins = (int)ns, ind = (int)nd;
+  const long long ss = ns * ns;
   double* R = h->d_rhs;
+  double* Y = h->d_rhs2;
   const double* corner = h->d_MF + mf_col_offset(sh, nt);
   for (long long i = 0; i < nt; ++i) {
-    const double* P = h->d_MF + mf_col_offset(sh, i);
-    const long long lda = mf_lda(sh, i);
-    if (i > 0) {
+    if (i > 0) {  // b_i -= L_{i,i-1} y_{i-1}   (RGF.H:365)
       const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
-      gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 0, R + (i - 1) * ns, n, 0,
-                 R + i * ns, n, R + i * ns, n, -1.0, 1.0), SMALL);       // RGF.H:365
+      gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 0, Y + (i - 1) * ns, n, 0,
+                 R + i * ns, n, R + i * ns, n, -1.0, 1.0), SMALL);
     }
-    trsv_lower(h, P, lda, ins, R + i * ns, n, nrhs);                      // RGF.H:356,367
+    // y_i = L_ii^{-1} b_i = U_i^T b_i   (RGF.H:356, 367)
+    GemmDesc g = mk(ins, nrhs, ins, h->d_U + i * ss, ns, 1, R + i * ns, n, 0, nullptr, 0,
+                    Y + i * ns, n, 1.0, 0.0);
+    g.triA = TRI_LOWER;
+    gemm(h, g, SMALL);
   }
   if (nd > 0) {
-    launch_arrow_gemv(sh, h->d_MF, R, n, nrhs, h->d_partial, h->stream);  // RGF.H:377-380
+    // b_d -= sum_i C_i y_i; y_d, then x_d, by the corner factor   (RGF.H:377-393)
+    launch_arrow_gemv(sh, h->d_MF, Y, n, nrhs, h->d_partial, h->stream);
     launch_arrow_reduce(sh, h->d_partial, nrhs, R, n, h->stream);
     h->kernels_issued += 2;
-    trsv_lower(h, corner, nd, ind, R + nt * ns, n, nrhs);                 // RGF.H:382
-    trsv_lower_t(h, corner, nd, ind, R + nt * ns, n, nrhs);               // RGF.H:393
-    // rhs_i -= C_i^T rhs_d for every block column (RGF.H:396-399)
+    trsv_lower(h, corner, nd, ind, R + nt * ns, n, nrhs);
+    trsv_lower_t(h, corner, nd, ind, R + nt * ns, n, nrhs);
+    // y_i -= C_i^T x_d for every block column (RGF.H:396-399)
     if (nt > 1) {
-      GemmDesc g = mk(ins, nrhs, ind, h->d_MF + 2 * ns, 2 * ns + nd, 1, R + nt * ns, n, 0, R, n, R,
+      GemmDesc g = mk(ins, nrhs, ind, h->d_MF + 2 * ns, 2 * ns + nd, 1, R + nt * ns, n, 0, Y, n, Y,
                       n, -1.0, 1.0);
       g.batch = (int)(nt - 1); g.sA = ns * (2 * ns + nd); g.sB = 0; g.sC = g.sD = ns;
       gemm(h, g, SMALL);
     }
     const double* Pl = h->d_MF + mf_col_offset(sh, nt - 1);
-    gemm(h, mk(ins, nrhs, ind, Pl + ns, ns + nd, 1, R + nt * ns, n, 0, R + (nt - 1) * ns, n,
-               R + (nt - 1) * ns, n, -1.0, 1.0), SMALL);
+    gemm(h, mk(ins, nrhs, ind, Pl + ns, ns + nd, 1, R + nt * ns, n, 0, Y + (nt - 1) * ns, n,
+               Y + (nt - 1) * ns, n, -1.0, 1.0), SMALL);
   }
   for (long long i = nt - 1; i >= 0; --i) {
-    const double* P = h->d_MF + mf_col_offset(sh, i);
-    trsv_lower_t(h, P, mf_lda(sh, i), ins, R + i * ns, n, nrhs);          // RGF.H:408,417
-    if (i > 0) {
-      const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
-      gemm(h, mk(ins, nrhs, ins, Pm + ns, mf_lda(sh, i - 1), 1, R + i * ns, n, 0,
-                 R + (i - 1) * ns, n, R + (i - 1) * ns, n, -1.0, 1.0), SMALL);  // RGF.H:410
+    if (i < nt - 1) {  // y_i -= L_{i+1,i}^T x_{i+1}   (RGF.H:410)
+      const double* P = h->d_MF + mf_col_offset(sh, i);
+      gemm(h, mk(ins, nrhs, ins, P + ns, mf_lda(sh, i), 1, R + (i + 1) * ns, n, 0, Y + i * ns, n,
+                 Y + i * ns, n, -1.0, 1.0), SMALL);
     }
+    // x_i = L_ii^{-T} y_i = U_i y_i   (RGF.H:408, 417)
+    GemmDesc g = mk(ins, nrhs, ins, h->d_U + i * ss, ns, 0, Y + i * ns, n, 0, nullptr, 0,
+                    R + i * ns, n, 1.0, 0.0);
+    g.triA = TRI_UPPER;
+    gemm(h, g, SMALL);
   }
 }
 
@@ -678,6 +702,7 @@ int ensure_factored(rgf_handle* h) {
   if (st) return st;
   h->factored = true;
   h->selinv_done = false;
+  h->inv_done = false;
   return RGF_OK;
 }
 
@@ -704,6 +729,22 @@ int ensure_selinv(rgf_handle* h) {
   st = sync_and_check(h);
   if (st) return st;
   h->selinv_done = true;
+  h->inv_done = true;
+  return RGF_OK;
+}
+
+// The diagonal-block inverses the solve uses (computed by the selected
+// inversion too).
+int ensure_inverses(rgf_handle* h) {
+  int st = ensure_factored(h);
+  if (st) return st;
+  if (h->inv_done) return RGF_OK;
+  if ((st = alloc_selinv(h))) return st;
+  st = run_stage(h, &h->g_inv, &h->k_inv, &h->runs_inv, [&] { issue_inverses(h); });
+  if (st) return st;
+  st = sync_and_check(h);
+  if (st) return st;
+  h->inv_done = true;
   return RGF_OK;
 }
 
@@ -720,6 +761,7 @@ void release(rgf_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->g_factor) cudaGraphExecDestroy(h->g_factor);
   if (h->g_selinv) cudaGraphExecDestroy(h->g_selinv);
+  if (h->g_inv) cudaGraphExecDestroy(h->g_inv);
   for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
   for (auto& e : h->ev_used) { cudaEventDestroy(e.e0); cudaEventDestroy(e.e1); }
   for (auto& e : h->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -727,7 +769,7 @@ void release(rgf_handle* h) {
   delete h->split_side;
   void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
                   h->d_logpart, h->d_scalars, h->d_diag, h->d_status, h->d_rhs, h->d_partial,
-                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side, h->d_ref};
+                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side, h->d_ref, h->d_rhs2};
   for (void* p : bufs) dfree(p);
   if (h->side) cudaStreamSynchronize(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -911,7 +953,7 @@ int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
   if (nrhs == 0) return RGF_OK;
   if (nrhs > 4096) return RGF_EINVAL;
   if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
-  int st = ensure_factored(h);
+  int st = ensure_inverses(h);
   if (st) return st;
   const long long n = h->sh.n;
   const size_t need = (size_t)n * nrhs;
@@ -919,9 +961,12 @@ int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
     for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
     h->g_solve.clear();
     dfree(h->d_rhs);
-    h->device_bytes -= h->rhs_cap * sizeof(double);
+    dfree(h->d_rhs2);
+    h->d_rhs2 = nullptr;
+    h->device_bytes -= 2 * h->rhs_cap * sizeof(double);
     h->rhs_cap = 0;
     if ((st = dalloc(h, &h->d_rhs, need))) return st;
+    if ((st = dalloc(h, &h->d_rhs2, need))) return st;
     h->rhs_cap = need;
   }
   const size_t pneed = (size_t)h->sh.nt * nrhs * std::max<long long>(1, h->sh.nd);
@@ -1281,6 +1326,7 @@ int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag) {
       if ((st = sync_and_check(h))) return st;
       h->factored = true;
       h->selinv_done = true;
+      h->inv_done = true;
     }
   } else {
     for (rgf_handle* h : b->h) {
