@@ -525,7 +525,11 @@ def run_rgf(args, w):
         ach = sp["tensor_flops"] / (sp["ms"] * 1e-3) / 1e12
         roofline = {"bound": "tensor", "kernel": "split_gemm_kernel (tcgen05 bf16 slices)",
                     "achieved": ach, "peak": peaks["bf16_sustained"], "unit": "TFLOP/s",
-                    "frac": ach / peaks["bf16_sustained"], "traffic": None,
+                    "frac": ach / peaks["bf16_sustained"],
+                    # dram read + write of one 2000x2000x2000 launch (ncu --set full,
+                    # python -m rgf_gb300.gemm_bench --m 2000 --k 2000 --syrk); operands
+                    # are read about once, the slices stay in L2
+                    "traffic": 81.6e6, "traffic_unit": "bytes per 2000^3 launch",
                     "peak_source": f"bf16 sustained, {src}",
                     "achieved_counts": "executed bf16 slice-product flops (pairs x 2MNK) / "
                                        "kernel time incl. slicing",
