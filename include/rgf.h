@@ -86,6 +86,29 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a,
                size_t ns, size_t nt, size_t nd,
                const rgf_opts* opts, rgf_handle** out);
 
+/* RGF<complex<double>> (RGF.H:756-774) for a Hermitian positive-definite
+ * A = X + iY: ia/ja as for rgf_create, a holds nnz complex values as
+ * interleaved (re, im) doubles.  The instance is held as the real symmetric
+ * embedding [[X, -Y], [Y, X]] ordered per block, itself a BTA matrix with
+ * (2ns, nt, 2nd), so every kernel and option of the real path applies.  On
+ * such a handle rgf_logdet returns log det A (= log det of the embedding / 2),
+ * and rgf_solve (x, b: n x nrhs complex), rgf_diag (diag: n complex, zero
+ * imaginary parts) and rgf_residual_norm[_normalized] take complex
+ * interleaved arrays; rgf_get_info, the exports and the device pointers
+ * describe the real embedding.  (The reference's RGF<CPX> pairs a Hermitian
+ * POTRF with plain transposes, which is consistent only for real data; this
+ * is the Hermitian factorization.) */
+int rgf_create_hermitian(const size_t* ia, const size_t* ja, const double* a,
+                         size_t ns, size_t nt, size_t nd,
+                         const rgf_opts* opts, rgf_handle** out);
+
+/* The embedding itself, on the host: the lower CSC (2n + 1 column pointers,
+ * *nnz2 entries) of the real matrix rgf_create_hermitian factors.  With ia2,
+ * ja2 and a2 NULL only *nnz2 is set (then call again with arrays of that size). */
+int rgf_hermitian_embed(const size_t* ia, const size_t* ja, const double* a,
+                        size_t ns, size_t nt, size_t nd,
+                        size_t* ia2, size_t* ja2, double* a2, size_t* nnz2);
+
 /* Replaces RGF<double>::~RGF (RGF.H:150-170). */
 int rgf_destroy(rgf_handle* h);
 

@@ -75,6 +75,12 @@ _SIGS = {
     "rgf_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
                              C.c_size_t, C.POINTER(_Opts), C.POINTER(C.c_void_p)]),
     "rgf_destroy": (C.c_int, [C.c_void_p]),
+    "rgf_create_hermitian": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                       C.c_size_t, C.c_size_t, C.POINTER(_Opts),
+                                       C.POINTER(C.c_void_p)]),
+    "rgf_hermitian_embed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                      C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.POINTER(C.c_size_t)]),
     "rgf_factorize": (C.c_int, [C.c_void_p]),
     "rgf_logdet": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "rgf_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
@@ -130,6 +136,27 @@ def load_library(path: str | None = None):
     return lib
 
 
+def hermitian_embed(ia, ja, a, ns: int, nt: int, nd: int):
+    """Lower CSC (ia2, ja2, a2) of the real symmetric embedding that a
+    Hermitian instance factors: [[X, -Y], [Y, X]] for A = X + iY, unknowns
+    ordered per block (Re then Im of each block, then of the arrowhead), a BTA
+    matrix with (2ns, nt, 2nd).  Host only."""
+    lib = load_library()
+    ia = np.ascontiguousarray(ia, dtype=np.uint64)
+    ja = np.ascontiguousarray(ja, dtype=np.uint64)
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    nnz2 = C.c_size_t()
+    _check(lib.rgf_hermitian_embed(_ptr(ia), _ptr(ja), _ptr(a), ns, nt, nd, None, None, None,
+                                   C.byref(nnz2)), "rgf_hermitian_embed")
+    n2 = 2 * (ns * nt + nd)
+    ia2 = np.empty(n2 + 1, dtype=np.uint64)
+    ja2 = np.empty(nnz2.value, dtype=np.uint64)
+    a2 = np.empty(nnz2.value, dtype=np.float64)
+    _check(lib.rgf_hermitian_embed(_ptr(ia), _ptr(ja), _ptr(a), ns, nt, nd, _ptr(ia2), _ptr(ja2),
+                                   _ptr(a2), C.byref(nnz2)), "rgf_hermitian_embed")
+    return ia2, ja2, a2
+
+
 def measure_fp64_peak() -> float:
     """FP64 (DMMA) TFLOP/s of the current GPU, measured by the library."""
     lib = load_library()
@@ -163,7 +190,9 @@ class RGF:
 
     ``ia``/``ja`` are the column pointers and row indices (``size_t``) and
     ``a`` the values of the matrix's lower triangle in CSC form.  Unlike the
-    reference, the arrays are copied to the device at construction.
+    reference, the arrays are copied to the device at construction.  A complex
+    ``a`` makes a Hermitian instance (``RGF<complex<double>>``, RGF.H:756-774):
+    logDet is then log det A and solve / RGFdiag take and return complex arrays.
     """
 
     def __init__(self, ia, ja, a, ns: int, nt: int, nd: int, precision: str = "fp64",
@@ -176,7 +205,8 @@ class RGF:
         self.n = self.ns * self.nt + self.nd
         self._ia = np.ascontiguousarray(ia, dtype=np.uint64)
         self._ja = np.ascontiguousarray(ja, dtype=np.uint64)
-        self._a = np.ascontiguousarray(a, dtype=np.float64)
+        self.hermitian = np.iscomplexobj(a)
+        self._a = np.ascontiguousarray(a, dtype=np.complex128 if self.hermitian else np.float64)
         if self._ia.size != self.n + 1:
             raise ValueError(f"ia must have n+1 = {self.n + 1} entries")
         nnz = int(self._ia[-1])
@@ -192,8 +222,10 @@ class RGF:
         # True/1: FP64-accurate emulated diagonal blocks, "native"/2: FP64
         # units, False/0: bulk slice count
         o.fp64_diag = {True: 1, False: 0, "native": 2}.get(fp64_diag, fp64_diag)
-        _check(lib.rgf_create(_ptr(self._ia), _ptr(self._ja), _ptr(self._a), self.ns, self.nt,
-                              self.nd, C.byref(o), C.byref(self._h)), "rgf_create")
+        create = lib.rgf_create_hermitian if self.hermitian else lib.rgf_create
+        _check(create(_ptr(self._ia), _ptr(self._ja), _ptr(self._a), self.ns, self.nt, self.nd,
+                      C.byref(o), C.byref(self._h)), "rgf_create")
+        self._dt = np.complex128 if self.hermitian else np.float64
 
     # -- reference methods ----------------------------------------------------
     def factorize(self) -> None:
@@ -211,11 +243,11 @@ class RGF:
         (RGF.H:559-578).  Arrays are n x nrhs column-major (ld = n); returns x."""
         if b is None:
             b = x
-        b = np.asarray(b, dtype=np.float64)
+        b = np.asarray(b, dtype=self._dt)
         if nrhs is None:
             nrhs = 1 if b.ndim == 1 else b.shape[1]
         bf = np.asfortranarray(b.reshape(self.n, nrhs) if b.ndim == 1 else b)
-        out = np.empty((self.n, nrhs), dtype=np.float64, order="F")
+        out = np.empty((self.n, nrhs), dtype=self._dt, order="F")
         _check(self._lib.rgf_solve(self._h, _ptr(out), _ptr(bf), int(nrhs)), "rgf_solve")
         if isinstance(x, np.ndarray) and x.size == out.size:
             if x.ndim == 1:
@@ -226,7 +258,7 @@ class RGF:
 
     def RGFdiag(self, diag=None) -> np.ndarray:
         """RGF.H:582-612: diag(A^{-1})."""
-        out = np.empty(self.n, dtype=np.float64)
+        out = np.empty(self.n, dtype=self._dt)
         _check(self._lib.rgf_diag(self._h, _ptr(out)), "rgf_diag")
         if diag is not None:
             diag[:] = out
@@ -234,8 +266,8 @@ class RGF:
 
     def residualNorm(self, x, b) -> float:
         """RGF.H:631-655 (first right-hand side)."""
-        xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
-        bb = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
+        xx = np.ascontiguousarray(np.asarray(x, dtype=self._dt).reshape(self.n, -1, order="F")[:, 0])
+        bb = np.ascontiguousarray(np.asarray(b, dtype=self._dt).reshape(self.n, -1, order="F")[:, 0])
         out = C.c_double()
         _check(self._lib.rgf_residual_norm(self._h, _ptr(xx), _ptr(bb), C.byref(out)),
                "rgf_residual_norm")
@@ -243,8 +275,8 @@ class RGF:
 
     def residualNormNormalized(self, x, b) -> float:
         """RGF.H:659-663."""
-        xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
-        bb = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(self.n, -1, order="F")[:, 0])
+        xx = np.ascontiguousarray(np.asarray(x, dtype=self._dt).reshape(self.n, -1, order="F")[:, 0])
+        bb = np.ascontiguousarray(np.asarray(b, dtype=self._dt).reshape(self.n, -1, order="F")[:, 0])
         out = C.c_double()
         _check(self._lib.rgf_residual_norm_normalized(self._h, _ptr(xx), _ptr(bb), C.byref(out)),
                "rgf_residual_norm_normalized")

@@ -39,6 +39,10 @@ struct rgf_handle {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool on_side = false;  // launch wrappers issue to `side`
   bool lookahead = true;
+  // complex Hermitian instance held as its real embedding (2ns, nt, 2nd):
+  // x, b and diag of the C ABI are then complex (interleaved re, im) of size nc
+  bool hermitian = false;
+  size_t hns = 0, hnt = 0, hnd = 0, nc = 0;
   BtaShape sh{};
   long long nnz = 0, mf_size = 0;
   rgf_opts opts{};
@@ -907,6 +911,26 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
   return RGF_OK;
 }
 
+int rgf_create_hermitian(const size_t* ia, const size_t* ja, const double* a, size_t ns,
+                         size_t nt, size_t nd, const rgf_opts* opts, rgf_handle** out) {
+  if (!out) return RGF_EINVAL;
+  *out = nullptr;
+  if (!ia || !ja || !a || ns < 1 || nt < 1) return RGF_EINVAL;
+  if (ns > (1u << 19) || nd > (1u << 19) || nt > (1u << 24)) return RGF_EINVAL;
+  if (validate_host_csc(ia, (long long)(ns * nt + nd))) return RGF_EINVAL;
+  std::vector<size_t> ia2, ja2;
+  std::vector<double> a2;
+  int st = hermitian_embed(ia, ja, a, ns, nt, nd, ia2, ja2, a2);
+  if (st) return st;
+  st = rgf_create(ia2.data(), ja2.data(), a2.data(), 2 * ns, nt, 2 * nd, opts, out);
+  if (st) return st;
+  rgf_handle* h = *out;
+  h->hermitian = true;
+  h->hns = ns; h->hnt = nt; h->hnd = nd;
+  h->nc = ns * nt + nd;
+  return RGF_OK;
+}
+
 int rgf_destroy(rgf_handle* h) {
   if (!h) return RGF_EINVAL;
   release(h);
@@ -927,6 +951,7 @@ int rgf_logdet(rgf_handle* h, double* logdet) {
   int st = ensure_factored(h);
   if (st) return st;
   RGF_CK(cudaMemcpy(logdet, h->d_scalars, sizeof(double), cudaMemcpyDeviceToHost));
+  if (h->hermitian) *logdet *= 0.5;  // det M = det(A)^2
   return RGF_OK;
 }
 
@@ -935,6 +960,15 @@ int rgf_diag(rgf_handle* h, double* diag) {
   if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
   int st = ensure_selinv(h);
   if (st) return st;
+  if (h->hermitian) {  // diag(A^{-1})_k = (M^{-1})_{Re k, Re k}, imaginary part 0
+    std::vector<double> d((size_t)h->sh.n);
+    RGF_CK(cudaMemcpy(d.data(), h->d_diag, sizeof(double) * d.size(), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < h->nc; ++k) {
+      diag[2 * k] = d[hermitian_real_index(h->hns, h->hnt, h->hnd, k, 0)];
+      diag[2 * k + 1] = 0.0;
+    }
+    return RGF_OK;
+  }
   RGF_CK(cudaMemcpy(diag, h->d_diag, sizeof(double) * h->sh.n, cudaMemcpyDeviceToHost));
   return RGF_OK;
 }
@@ -948,8 +982,40 @@ int rgf_diag_device(rgf_handle* h, const double** d_diag) {
   return RGF_OK;
 }
 
+// complex (interleaved) n_c x nrhs <-> real embedded 2 n_c x nrhs
+static void hermitian_to_real(const rgf_handle* h, const double* z, size_t nrhs, double* r) {
+  const size_t nc = h->nc, n2 = 2 * nc;
+  for (size_t q = 0; q < nrhs; ++q)
+    for (size_t k = 0; k < nc; ++k) {
+      r[q * n2 + hermitian_real_index(h->hns, h->hnt, h->hnd, k, 0)] = z[2 * (q * nc + k)];
+      r[q * n2 + hermitian_real_index(h->hns, h->hnt, h->hnd, k, 1)] = z[2 * (q * nc + k) + 1];
+    }
+}
+static void real_to_hermitian(const rgf_handle* h, const double* r, size_t nrhs, double* z) {
+  const size_t nc = h->nc, n2 = 2 * nc;
+  for (size_t q = 0; q < nrhs; ++q)
+    for (size_t k = 0; k < nc; ++k) {
+      z[2 * (q * nc + k)] = r[q * n2 + hermitian_real_index(h->hns, h->hnt, h->hnd, k, 0)];
+      z[2 * (q * nc + k) + 1] = r[q * n2 + hermitian_real_index(h->hns, h->hnt, h->hnd, k, 1)];
+    }
+}
+
+static int solve_real(rgf_handle* h, double* x, const double* b, size_t nrhs);
+
 int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
   if (!h || !x || !b) return RGF_EINVAL;
+  if (nrhs == 0) return RGF_OK;
+  if (nrhs > 4096) return RGF_EINVAL;
+  if (!h->hermitian) return solve_real(h, x, b, nrhs);
+  std::vector<double> br(2 * h->nc * nrhs), xr(2 * h->nc * nrhs);
+  hermitian_to_real(h, b, nrhs, br.data());
+  const int st = solve_real(h, xr.data(), br.data(), nrhs);
+  if (st) return st;
+  real_to_hermitian(h, xr.data(), nrhs, x);
+  return RGF_OK;
+}
+
+static int solve_real(rgf_handle* h, double* x, const double* b, size_t nrhs) {
   if (nrhs == 0) return RGF_OK;
   if (nrhs > 4096) return RGF_EINVAL;
   if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
@@ -1023,6 +1089,15 @@ int rgf_solve(rgf_handle* h, double* x, const double* b, size_t nrhs) {
 
 int rgf_residual_norm(rgf_handle* h, const double* x, const double* b, double* norm) {
   if (!h || !x || !b || !norm) return RGF_EINVAL;
+  if (h->hermitian) {  // ||b - A x|| = ||b' - M x'|| for the embedded vectors
+    std::vector<double> xr(2 * h->nc), br(2 * h->nc);
+    hermitian_to_real(h, x, 1, xr.data());
+    hermitian_to_real(h, b, 1, br.data());
+    h->hermitian = false;
+    const int st = rgf_residual_norm(h, xr.data(), br.data(), norm);
+    h->hermitian = true;
+    return st;
+  }
   if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
   const long long n = h->sh.n;
   int st;

@@ -1,6 +1,8 @@
 // Internal interfaces shared by the CUDA translation units of librgf_gb300.
 #pragma once
 
+#include <vector>
+
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
@@ -50,6 +52,16 @@ struct GemmDesc {
 // Algorithmic flops of one GemmDesc (triangular operands and lower-only
 // outputs counted at their LAPACK sizes).
 double gemm_flops(const GemmDesc& g);
+
+// ---- complex Hermitian matrices (hermitian.cu) -------------------------------
+// Lower CSC of the real symmetric embedding [[X, -Y], [Y, X]] of the Hermitian
+// A = X + iY given as its lower CSC (a: interleaved re, im), ordered so that it
+// is a BTA matrix with (2ns, nt, 2nd).
+int hermitian_embed(const size_t* ia, const size_t* ja, const double* a, size_t ns, size_t nt,
+                    size_t nd, std::vector<size_t>& ia2, std::vector<size_t>& ja2,
+                    std::vector<double>& a2);
+// Real index of Re (imag = 0) or Im (imag = 1) of complex unknown k.
+size_t hermitian_real_index(size_t ns, size_t nt, size_t nd, size_t k, int imag);
 
 // ---- FP64 kernels (k_fp64.cu) ---------------------------------------------
 // Returns the number of kernels launched (2 with split-K).

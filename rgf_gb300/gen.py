@@ -155,3 +155,48 @@ def generate_batch(count: int, seed: int, **kw):
         ia, ja, a = generate_bta(ns, nt, nd, seed * 100003 + i)
         out.append((ia, ja, a, ns, nt, nd))
     return out
+
+
+def generate_bta_hermitian(ns: int, nt: int, nd: int, seed: int):
+    """Return (ia, ja, a): lower CSC of a seeded Hermitian positive-definite
+    BTA matrix, ``a`` complex128.  Same structure and scales as generate_bta
+    with complex N(0, 1) draws: D_i = A_i A_i^H / ns + (ns + 2) I,
+    B_i ~ N(0, 0.1/ns), C_i ~ N(0, 0.1), corner R R^H / nd + (nt + 2) I.
+    Dense assembly: meant for test sizes."""
+    ns, nt, nd = int(ns), int(nt), int(nd)
+    rng = np.random.default_rng(seed)
+    n = ns * nt + nd
+
+    def cn(*shape):
+        return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2.0)
+
+    A = np.zeros((n, n), dtype=np.complex128)
+    for i in range(nt):
+        s = slice(i * ns, (i + 1) * ns)
+        G = cn(ns, ns)
+        A[s, s] = G @ G.conj().T / ns + (ns + 2.0) * np.eye(ns)
+        if i < nt - 1:
+            t = slice((i + 1) * ns, (i + 2) * ns)
+            A[t, s] = cn(ns, ns) * np.sqrt(0.1 / ns)
+        if nd:
+            A[nt * ns:, s] = cn(nd, ns) * np.sqrt(0.1)
+    if nd:
+        R = cn(nd, nd)
+        A[nt * ns:, nt * ns:] = R @ R.conj().T / nd + (nt + 2.0) * np.eye(nd)
+    A = np.tril(A)
+    A = A + np.tril(A, -1).conj().T
+    np.fill_diagonal(A, A.diagonal().real)
+    # lower CSC over the full block pattern (explicit zeros kept)
+    ia = np.zeros(n + 1, dtype=np.uint64)
+    rows, vals = [], []
+    for c in range(n):
+        if c < ns * nt:
+            i = c // ns
+            hi = (i + 2) * ns if i < nt - 1 else (i + 1) * ns
+            r = np.concatenate([np.arange(c, hi), np.arange(nt * ns, n)])
+        else:
+            r = np.arange(c, n)
+        rows.append(r)
+        vals.append(A[r, c])
+        ia[c + 1] = ia[c] + len(r)
+    return ia, np.concatenate(rows).astype(np.uint64), np.concatenate(vals)
