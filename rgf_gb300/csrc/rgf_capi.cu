@@ -294,9 +294,13 @@ void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, in
     upd(split_row, rows - split_row, BULK);
     h->on_side = false;
   }
-  if (h->split && h->opts.fp64_diag) {
+  if (h->split && h->opts.fp64_diag && cols - c1 > 256) {
     upd(c1, cols - c1, DIAG);              // inside the diagonal block: FP64 accuracy
     upd(cols, split_row - cols, BULK);
+  } else if (h->split && h->opts.fp64_diag) {
+    // a narrow node: both parts are FP64 products anyway, so one launch
+    // covers the diagonal block and the rows below it on the critical path
+    upd(c1, split_row - c1, SMALL);
   } else {
     upd(c1, split_row - c1, BULK);
   }
