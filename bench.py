@@ -578,7 +578,7 @@ def run_rgf(args, w):
                 "dtype": "f64" if args.precision == "fp64" else "bf16-slices/f64",
                 "data": "synthetic",
                 "config": {"workload": args.workload, **cfg_of(w), "precision": args.precision,
-                           "fp64_diag": not args.no_fp64_diag, "slices": args.slices or 6,
+                           "fp64_diag": not args.no_fp64_diag, "slices": args.slices or 5, "slice_bits": 8 * (args.slices or 5) - 1,
                            "l2": "inputs larger than L2 (CSC %.1f GB, factor %.1f GB)" % (
                                h2d / 1e9, s.info()["mf_size"] * 8 / 1e9)},
                 "e2e": ({"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
