@@ -191,9 +191,25 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
 // parallel pass at the end.  The log-determinant is summed later from the
 // factor's diagonal, off this path.
 // ---------------------------------------------------------------------------
-// reciprocal square root of a normal positive double: exponent split with
-// integer ops, an FP32 seed from the top mantissa bits (no FP64 conversion
-// instructions) and two Newton steps in FP64
+// float -> double by bit manipulation (no FP64 conversion instruction);
+// zero and subnormal floats give zero
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int ex = (u >> 23) & 0xffu;
+  if (ex == 0) return 0.0;
+  return __longlong_as_double((long long)((unsigned long long)(u >> 31) << 63 |
+                                          (unsigned long long)(ex - 127 + 1023) << 52 |
+                                          (unsigned long long)(u & 0x7fffffu) << 29));
+}
+
+// Reciprocal square root of a normal positive double with few dependent FP64
+// operations (they are the slow link of the leaf's pivot chain): d = m 4^k
+// with m in [1, 4) by integer ops; an FP32 seed y0 = rsqrt(m_hi) is refined
+// once in double-float arithmetic on the FP32 units (m = m_hi + m_lo split
+// exactly from the bit pattern; e = 1 - m y0^2 with FMA-exact products), which
+// gives ~44 bits; one FP64 Newton step then gives full precision.  FP64 ops on
+// the chain: one add, one multiply, two FMAs; the 4^-k scale is an exponent
+// shift.
 __device__ __forceinline__ double rsqrt_fast(double d) {
   const long long b = __double_as_longlong(d);
   const int e = (int)((b >> 52) & 0x7ff) - 1023;
@@ -201,17 +217,22 @@ __device__ __forceinline__ double rsqrt_fast(double d) {
   const int k = e >> 1;                                   // d = m * 4^k, m in [1, 4)
   const long long mb = b - ((long long)(2 * k) << 52);
   const double m = __longlong_as_double(mb);
-  // float with the same value as m up to 23 mantissa bits
-  const unsigned int fb = (unsigned int)(((mb >> 52) - 1023 + 127) << 23) |
-                          (unsigned int)((mb >> 29) & 0x7fffff);
-  const float yf = rsqrtf(__uint_as_float(fb));
-  const unsigned int yb = __float_as_uint(yf);
-  double y = __longlong_as_double((long long)(((yb >> 23) & 0xff) - 127 + 1023) << 52 |
-                                  ((long long)(yb & 0x7fffff) << 29));
-  const double hm = 0.5 * m;
-  y = y * fma(-hm, y * y, 1.5);
-  y = y * fma(-hm, y * y, 1.5);
-  return y * __longlong_as_double((long long)(1023 - k) << 52);
+  const int em = (int)((mb >> 52) & 0x7ff) - 1023;        // 0 or 1
+  // m_hi: the top 24 significant bits as a float; m_lo: the remaining 29 bits
+  const float mh = __uint_as_float((unsigned int)(((mb >> 52) - 1023 + 127) << 23) |
+                                   (unsigned int)((mb >> 29) & 0x7fffff));
+  const float ml = (float)(unsigned int)(mb & ((1ll << 29) - 1)) *
+                   __uint_as_float((unsigned int)(127 + em - 52) << 23);
+  const float y0 = rsqrtf(mh);
+  const float p = y0 * y0;
+  const float pe = fmaf(y0, y0, -p);                      // y0^2 = p + pe exactly
+  float t = fmaf(-mh, p, 1.0f);
+  t = fmaf(-mh, pe, t);
+  t = fmaf(-ml, p, t);                                    // e = 1 - m y0^2
+  const double y1 = f2d_bits(y0) + f2d_bits(0.5f * y0 * t);
+  const double hm = __longlong_as_double(mb - (1ll << 52));  // m / 2, exact
+  const double y2 = fma(y1, fma(-hm, y1 * y1, 0.5), y1);    // y1 (1.5 - m y1^2 / 2)
+  return __longlong_as_double(__double_as_longlong(y2) - ((long long)k << 52));
 }
 
 
