@@ -137,12 +137,6 @@ __global__ void copy_kernel(const double* X, long long ldx, double* Y, long long
   if (r < m && c < n) Y[r + (long long)c * ldy] = X[r + (long long)c * ldx];
 }
 
-__global__ void zero_upper_kernel(double* X, long long ld, int m, long long stride) {
-  X += (long long)blockIdx.z * stride;
-  const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
-  if (r < m && c < m && r < c) X[r + (long long)c * ld] = 0.0;
-}
-
 // y = A x with A symmetric, stored as its lower CSC: column c contributes
 // a_rc x_c to y_r (scatter) and, off the diagonal, a_rc x_r to y_c (gather).
 __global__ void sym_spmv_kernel(long long n, const size_t* __restrict__ ia,
@@ -253,13 +247,6 @@ void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m
   if (m <= 0 || n <= 0 || batch <= 0) return;
   dim3 grid((m + 31) / 32, (n + 7) / 8, batch);
   copy_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ldx, Y, ldy, m, n, sX, sY);
-}
-
-void launch_zero_upper(double* X, long long ld, int m, int batch, long long stride,
-                       cudaStream_t s) {
-  if (m <= 0 || batch <= 0) return;
-  dim3 grid((m + 31) / 32, (m + 7) / 8, batch);
-  zero_upper_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ld, m, stride);
 }
 
 // r = b - y; x += d (element-wise over len entries)

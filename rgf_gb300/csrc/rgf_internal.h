@@ -109,9 +109,6 @@ void launch_set_identity(double* X, long long ld, int m, int batch, long long st
 // Y (m x n, ldy) = X (m x n, ldx); batched
 void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,
                  int batch, long long sX, long long sY, cudaStream_t s);
-// zero the strict upper triangle of an m x m block; batched
-void launch_zero_upper(double* X, long long ld, int m, int batch, long long stride,
-                       cudaStream_t s);
 // r = b - A x (symmetric, from the lower CSC) for the first column; then
 // out[0] = ||r||_2, out[1] = ||b||_2.  scratch: n doubles.
 void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
