@@ -50,6 +50,22 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's value (the job's time is the last rank to finish)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(flops_per_replica: float, world_size: int, ms_step: float) -> float:
+    """Whole-job FP64-equivalent TFLOP/s of world_size replicas that each did
+    flops_per_replica in (at most) ms_step."""
+    return flops_per_replica * world_size / (ms_step * 1e-3) / 1e12
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -456,12 +472,9 @@ def run_rgf(args, w):
     torch.cuda.synchronize()
     timer = s.kernel_timer_read(reset=True)
     s.kernel_timer(False)
-    if dist:
-        t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(ms_total, dist, "cuda")
     ms_step = ms_total / args.steps
-    value = flops * ws / (ms_step * 1e-3) / 1e12
+    value = replica_throughput(flops, ws, ms_step)
 
     # end-to-end through the public API: host CSC -> device, diag -> host
     e2e_ms = []
@@ -486,9 +499,7 @@ def run_rgf(args, w):
                          "logdet_rgfdiag_d2h_ms": (t3 - t2) * 1e3, "destroy_ms": (t4 - t3) * 1e3}
     e2e_med = statistics.median(e2e_ms) if e2e_ms else float("nan")
     if dist and e2e_ms:
-        t = torch.tensor([max(e2e_ms)], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_med = float(t.item())
+        e2e_med = max_over_ranks(max(e2e_ms), dist, "cuda")
     h2d = ia_p.nbytes + ja_p.nbytes + a_p.nbytes
     d2h = diag_host.nbytes + 8
 
