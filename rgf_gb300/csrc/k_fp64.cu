@@ -426,7 +426,8 @@ __global__ void __launch_bounds__(128) gemm_thin_m_kernel(GemmDesc g, int kchunk
 // Thin products (n <= 16, op(B) = B): thread = output row; the CTA's 128 rows
 // share 32-term K tiles of op(A) and op(B) staged through shared memory (read
 // along A's contiguous dimension either way), so every FP64 instruction has
-// all lanes busy.  blockIdx.y selects a K chunk; partial sums go to the
+// all lanes busy.  The next tile is loaded into registers while the current
+// one is multiplied.  blockIdx.y selects a K chunk; partial sums go to the
 // split-K workspace in the GEMM kernel's layout.  op(A) may be triangular.
 __global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk) {
   __shared__ double As[32][129];
@@ -439,8 +440,11 @@ __global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk
   double acc[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) acc[c] = 0.0;
-  for (int kt = k0; kt < k1; kt += 32) {
-    for (int idx = tid; idx < 32 * 128; idx += 128) {
+  double ra[32], rb[4];
+  auto load = [&](int kt) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int idx = tid + 128 * j;
       int i, kk;
       if (!g.transA) { i = idx & 127; kk = idx >> 7; }
       else           { kk = idx & 31; i = idx >> 5; }
@@ -451,21 +455,42 @@ __global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk
       double v = 0.0;
       if (ok) v = g.transA ? g.A[(long long)kg + (long long)row * g.lda]
                            : g.A[(long long)row + (long long)kg * g.lda];
-      As[kk][i] = v;
+      ra[j] = v;
     }
-    for (int idx = tid; idx < 32 * 16; idx += 128) {
-      const int kk = idx & 31, c = idx >> 5, kg = kt + kk;
-      Bs[kk][c] = (c < g.n && kg < k1) ? g.B[(long long)kg + (long long)c * g.ldb] : 0.0;
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int kk = 0; kk < 32; ++kk) {
-      const double a = As[kk][tid];
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
-        if (c < g.n) acc[c] = fma(a, Bs[kk][c], acc[c]);
+    for (int j = 0; j < 4; ++j) {
+      const int idx = tid + 128 * j, kk = idx & 31, c = idx >> 5, kg = kt + kk;
+      rb[j] = (c < g.n && kg < k1) ? g.B[(long long)kg + (long long)c * g.ldb] : 0.0;
     }
-    __syncthreads();
+  };
+  auto store = [&]() {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int idx = tid + 128 * j;
+      if (!g.transA) As[idx >> 7][idx & 127] = ra[j];
+      else           As[idx & 31][idx >> 5] = ra[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int idx = tid + 128 * j;
+      Bs[idx & 31][idx >> 5] = rb[j];
+    }
+  };
+  if (k0 < k1) {
+    load(k0);
+    for (int kt = k0; kt < k1; kt += 32) {
+      store();
+      __syncthreads();
+      if (kt + 32 < k1) load(kt + 32);
+#pragma unroll 4
+      for (int kk = 0; kk < 32; ++kk) {
+        const double a = As[kk][tid];
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (c < g.n) acc[c] = fma(a, Bs[kk][c], acc[c]);
+      }
+      __syncthreads();
+    }
   }
   if (r < g.m) {
     double* W = g.ws + (long long)blockIdx.y * g.m * g.n;
@@ -520,7 +545,8 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
   if (g.n <= 16 && !g.transB && g.triB == TRI_NONE && g.batch == 1 && g.ws && !g.outLower &&
       !g.A2) {
     const int rb = (g.m + 127) / 128;
-    int kchunks = std::max(1, std::min((2 * 152 + rb - 1) / rb, (g.k + 31) / 32));
+    // about two CTAs per SM, each with at least 2 K tiles to pipeline
+    int kchunks = std::max(1, std::min((2 * 152 + rb - 1) / rb, (g.k + 63) / 64));
     while (kchunks > 1 && (long long)kchunks * g.m * g.n > g.ws_elems) --kchunks;
     if ((long long)kchunks * g.m * g.n <= g.ws_elems) {
       const int kchunk = ((g.k + kchunks - 1) / kchunks + 31) / 32 * 32;
