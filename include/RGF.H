@@ -60,11 +60,7 @@ class RGF<double> {
   RGF(size_t* ia, size_t* ja, double* a, size_t ns, size_t nt, size_t nd)
       : ia_(ia), ja_(ja), a_(a), n_(ns * nt + nd), h_(NULL) {
     rgf_opts o;
-    rgf_default_opts(&o);
-    const char* sel = std::getenv("RGF_GB300_SELINV");
-    if (sel && std::strcmp(sel, "compat") == 0) o.selinv_mode = RGF_SELINV_COMPAT;
-    const char* prec = std::getenv("RGF_GB300_PRECISION");
-    if (prec && std::strcmp(prec, "split") == 0) o.precision = RGF_PREC_SPLIT;
+    rgf_gb300_detail::env_opts(&o);
     check(rgf_create(ia, ja, a, ns, nt, nd, &o, &h_), "RGF::RGF");
   }
 
@@ -111,9 +107,7 @@ class RGF<double> {
   RGF(const RGF&);
   RGF& operator=(const RGF&);
 
-  static void check(int status, const char* what) {
-    if (status != RGF_OK) throw std::runtime_error(std::string(what) + ": " + rgf_status_string(status));
-  }
+  static void check(int status, const char* what) { rgf_gb300_detail::check(status, what); }
 
   size_t* ia_;
   size_t* ja_;
