@@ -11,7 +11,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_MAIN = "/root/reference/main.C"
+REF_MAIN = os.path.join(os.environ.get("RGF_REFERENCE", "/root/reference"), "main.C")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_MAIN), reason="reference sources not present")
