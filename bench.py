@@ -220,31 +220,52 @@ def run_batch(args):
                            device=torch.cuda.current_device(),
                            fp64_diag=not args.no_fp64_diag)
     stream = torch.cuda.ExternalStream(b.stream())
-    for _ in range(args.warmup):
-        b.run(concurrent=True, want_diag=False)
-    k0 = b.kernels()
-    clocks = Clocks(torch.cuda.current_device())
-    torch.cuda.synchronize()
-    clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        b.run(concurrent=True, want_diag=False)
-    e1.record(stream); e1.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    launches = (b.kernels() - k0) // args.steps
+
+    def timed():
+        for _ in range(args.warmup):
+            b.run(concurrent=True, want_diag=False)
+        k0 = b.kernels()
+        clocks = Clocks(torch.cuda.current_device())
+        torch.cuda.synchronize()
+        clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            b.run(concurrent=True, want_diag=False)
+        e1.record(stream); e1.synchronize()
+        return e0.elapsed_time(e1) / args.steps, (b.kernels() - k0) // args.steps, clocks.stop()
+
+    ms, launches, clk = timed()
+    tune = None
+    if args.autotune:
+        # the same batch again after the autotuner picked each (ns, nd)
+        # class's knobs (leaf width, look-ahead, routing bias)
+        ms_default = ms
+        t0 = time.perf_counter()
+        classes = b.autotune()
+        tune_s = time.perf_counter() - t0
+        ms, launches, clk = timed()
+        choices = {}
+        for (s_, _, d_), t in zip(b.sizes, b.tunings()):
+            choices[f"ns{s_}_nd{d_}"] = [t["leaf_nb"], t["lookahead"], t["split_bias"]]
+        tune = {"classes": classes, "tune_s": tune_s, "default_ms_per_step": ms_default,
+                "default_value": flops / (ms_default * 1e-3) / 1e12,
+                "choices_leaf_nb_lookahead_bias": choices}
     # per-instance launches (each instance's own stage graphs, one after another)
-    b.run(concurrent=False, want_diag=False)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    b.run(concurrent=False, want_diag=False)
-    ms_serial = (time.perf_counter() - t0) * 1e3
+    ms_serial = None
+    if not args.no_per_instance:
+        b.run(concurrent=False, want_diag=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run(concurrent=False, want_diag=False)
+        ms_serial = (time.perf_counter() - t0) * 1e3
     # end to end: host CSC -> device for every instance, diag back to host
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b2 = rgf_gb300.RGFBatch(inst, precision=args.precision, slices=args.slices,
                             device=torch.cuda.current_device(), fp64_diag=not args.no_fp64_diag)
+    if args.autotune:
+        b2.autotune()  # the choices cached by the first batch
     _, diags = b2.run(concurrent=True, want_diag=True)
     b2.close()
     ms_e2e = (time.perf_counter() - t0) * 1e3
@@ -262,14 +283,17 @@ def run_batch(args):
                            "ns_choices": [42, 128, 256, 512], "nt_range": [3, 60],
                            "nd_choices": [0, 2, 6], "precision": args.precision,
                            "execution": "one captured CUDA graph, one concurrent branch per instance",
+                           "autotune": bool(args.autotune),
                            "l2": "inputs larger than L2 (%.1f GB CSC)" % (h2d / 1e9)},
-                "per_instance_launches": {"value": flops / (ms_serial * 1e-3) / 1e12,
-                                          "ms_per_step": ms_serial},
-                "speedup_vs_per_instance": ms_serial / ms,
+                "per_instance_launches": None if ms_serial is None else {
+                    "value": flops / (ms_serial * 1e-3) / 1e12, "ms_per_step": ms_serial},
+                "speedup_vs_per_instance": None if ms_serial is None else ms_serial / ms,
                 "e2e": {"value": flops / (ms_e2e * 1e-3) / 1e12, "unit": "TFLOP/s",
                         "ms_per_step": ms_e2e, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "clocks": clk}
+        if tune is not None:
+            line["autotune"] = tune
         print(json.dumps(line), flush=True)
 
 
@@ -625,6 +649,11 @@ def main():
                    help="factors made resident before the request stream starts")
     p.add_argument("--serve-budget-gb", type=float, default=160.0)
     p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--no-per-instance", action="store_true",
+                   help="batch workload: skip the instance-after-instance comparison run")
+    p.add_argument("--autotune", action="store_true",
+                   help="batch workload: time the default knobs, autotune every (ns, nd) "
+                        "class, then time again (reported as the line's value)")
     p.add_argument("--precision", choices=["fp64", "split"], default="split")
     p.add_argument("--no-fp64-ref", action="store_true",
                    help="skip the plain-FP64 comparison run (1 warm-up + 1 step)")

@@ -237,6 +237,55 @@ int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag);
 /* GPU kernels launched by the batch's runs so far. */
 int rgf_batch_kernels(rgf_batch* b, long long* kernels);
 
+/* ---- tuning -----------------------------------------------------------------
+ * Knobs of one handle's factorize + selected inversion (no counterpart in the
+ * reference, whose MAGMA calls pick their own blocking).  None changes the
+ * algorithm or the operation count; each changes how it is cut into kernels:
+ *   leaf_nb     column width of the FP64 leaf Cholesky / triangular solves
+ *               the recursive panel factorization bottoms out in: 16, 32, 64;
+ *   lookahead   1 = the rows below each diagonal block are solved and updated
+ *               on a second, lower-priority stream; 0 = one stream;
+ *   split_bias  split precision: a product runs on the tensor cores when its
+ *               estimated split time times split_bias is below its estimated
+ *               FP64 time (1.0 = the fitted cost model; > 1 moves products to
+ *               the FP64 kernels).  In [1/16, 16].
+ * Results under different knobs agree to rounding; under the same knobs they
+ * are bitwise identical, alone, batched or served. */
+typedef struct rgf_tuning {
+  int leaf_nb;
+  int lookahead;
+  double split_bias;
+  double ms;        /* out: factorize + RGFdiag time measured by the autotuner
+                       for this choice (0 when not measured)                 */
+  int reserved[4];
+} rgf_tuning;
+
+enum rgf_tune_flags {
+  RGF_TUNE_FORCE = 1  /* measure again even when the process-wide cache holds
+                         a choice for this class                            */
+};
+
+int rgf_get_tuning(rgf_handle* h, rgf_tuning* t);
+/* Set the knobs (t->ms is ignored).  Stage graphs captured with the old knobs
+ * are dropped, the factor and selected inverse are recomputed on next use,
+ * and a batch holding the handle recaptures its graph on its next run. */
+int rgf_set_tuning(rgf_handle* h, const rgf_tuning* t);
+/* Autotuner: times factorize + selected inversion (graph-replayed, best of two
+ * after a direct run and a capture) for candidate knobs by coordinate
+ * descent (leaf width, then look-ahead, then, in split precision, the routing
+ * bias), keeps a candidate only when it is at least 2% faster, and sets the
+ * best on h.  Choices are cached per process by (device, ns, nd, options);
+ * a cached class is not measured again unless flags has RGF_TUNE_FORCE.
+ * Allocates the selected-inversion buffers; leaves h unfactored.  The matrix
+ * must be positive definite (the status of a failed run is returned, with
+ * the knobs left as they were).  RGF_EINVAL while the kernel timer is on
+ * (timed stages run launch by launch).  chosen may be NULL. */
+int rgf_autotune(rgf_handle* h, int flags, rgf_tuning* chosen);
+/* Autotune a batch: instances are grouped by (ns, nd); each group's knobs
+ * are tuned (or taken from the cache) on its instance of median nt and set on
+ * every member.  *classes (may be NULL) receives the number of groups. */
+int rgf_batch_autotune(rgf_batch* b, int flags, size_t* classes);
+
 /* ---- request loop (serving) -------------------------------------------------
  * Continuous batching on one GPU: `slots` workers take requests as soon as
  * they are free and, for a new factorization, as soon as its HBM footprint

@@ -58,6 +58,25 @@ class _Request(C.Structure):
                 ("reserved_bytes", C.c_size_t)]
 
 
+class _Tuning(C.Structure):
+    _fields_ = [("leaf_nb", C.c_int), ("lookahead", C.c_int), ("split_bias", C.c_double),
+                ("ms", C.c_double), ("reserved", C.c_int * 4)]
+
+
+TUNE_FORCE = 1
+
+
+def _tuning_dict(t: _Tuning) -> dict:
+    return {"leaf_nb": t.leaf_nb, "lookahead": t.lookahead, "split_bias": t.split_bias,
+            "ms": t.ms}
+
+
+def _tuning_struct(leaf_nb: int, lookahead: int, split_bias: float) -> _Tuning:
+    t = _Tuning()
+    t.leaf_nb, t.lookahead, t.split_bias = int(leaf_nb), int(lookahead), float(split_bias)
+    return t
+
+
 class _ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong),
                 ("completed", C.c_longlong), ("failed", C.c_longlong),
@@ -114,6 +133,10 @@ _SIGS = {
                                    C.c_int, C.c_double, C.c_void_p, C.c_int, C.c_void_p]),
     "rgf_kernel_timer_read": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double),
                                         C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+    "rgf_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(_Tuning)]),
+    "rgf_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(_Tuning)]),
+    "rgf_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_Tuning)]),
+    "rgf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
 }
 
 
@@ -174,6 +197,12 @@ def dgemm_device(precision: str, transa: str, transb: str, m: int, n: int, k: in
                                 transb.encode(), m, n, k, alpha, C.c_void_p(A_ptr), lda,
                                 C.c_void_p(B_ptr), ldb, beta, C.c_void_p(C_ptr), ldc,
                                 C.c_void_p(stream)), "rgf_dgemm_device")
+
+
+def _tuning_of(lib, h) -> dict:
+    t = _Tuning()
+    _check(lib.rgf_get_tuning(h, C.byref(t)), "rgf_get_tuning")
+    return _tuning_dict(t)
 
 
 def _check(status: int, what: str) -> None:
@@ -313,6 +342,25 @@ class RGF:
         _check(self._lib.rgf_get_stream(self._h, C.byref(p)), "rgf_get_stream")
         return p.value or 0
 
+    def tuning(self) -> dict:
+        """The knobs of this instance: leaf_nb, lookahead, split_bias and the
+        autotuner's measured factorize + RGFdiag time ``ms`` (0 if none)."""
+        return _tuning_of(self._lib, self._h)
+
+    def set_tuning(self, leaf_nb: int = 32, lookahead: int = 1, split_bias: float = 1.0) -> None:
+        """Set the knobs (leaf_nb 16/32/64, lookahead 0/1, split_bias in
+        [1/16, 16]); the factor is recomputed on next use."""
+        t = _tuning_struct(leaf_nb, lookahead, split_bias)
+        _check(self._lib.rgf_set_tuning(self._h, C.byref(t)), "rgf_set_tuning")
+
+    def autotune(self, force: bool = False) -> dict:
+        """Measure candidate knobs on this instance (or take the process-wide
+        cached choice for its class) and keep the fastest; returns it."""
+        t = _Tuning()
+        _check(self._lib.rgf_autotune(self._h, TUNE_FORCE if force else 0, C.byref(t)),
+               "rgf_autotune")
+        return _tuning_dict(t)
+
     def kernel_timer(self, enable) -> None:
         """True/1: time bulk GEMMs; 2: also print per-shape totals on reset."""
         _check(self._lib.rgf_kernel_timer_enable(self._h, int(enable)), "timer")
@@ -410,6 +458,30 @@ class RGFBatch:
         k = C.c_longlong()
         _check(self._lib.rgf_batch_kernels(self._h, C.byref(k)), "rgf_batch_kernels")
         return k.value
+
+    def autotune(self, force: bool = False) -> int:
+        """Tune every (ns, nd) class of the batch on its instance of median nt
+        (or take the cached choice) and set it on all members; returns the
+        number of classes."""
+        n = C.c_size_t()
+        _check(self._lib.rgf_batch_autotune(self._h, TUNE_FORCE if force else 0, C.byref(n)),
+               "rgf_batch_autotune")
+        return n.value
+
+    def _handle(self, i: int) -> C.c_void_p:
+        h = C.c_void_p()
+        _check(self._lib.rgf_batch_handle(self._h, int(i), C.byref(h)), "rgf_batch_handle")
+        return h
+
+    def tunings(self) -> list:
+        """The knobs of every instance (see :meth:`RGF.tuning`)."""
+        return [_tuning_of(self._lib, self._handle(i)) for i in range(self.count)]
+
+    def set_tuning(self, i: int, leaf_nb: int = 32, lookahead: int = 1,
+                   split_bias: float = 1.0) -> None:
+        """Set the knobs of instance i; the batch graph is captured again."""
+        t = _tuning_struct(leaf_nb, lookahead, split_bias)
+        _check(self._lib.rgf_set_tuning(self._handle(i), C.byref(t)), "rgf_set_tuning")
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:

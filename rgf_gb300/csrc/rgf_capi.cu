@@ -9,14 +9,17 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/rgf.h"
@@ -89,7 +92,12 @@ struct rgf_handle {
 
   SplitEngine* split = nullptr;
   SplitEngine* split_side = nullptr;  // own slice workspace for the side stream
-  int nb = 32;  // leaf width of the panel Cholesky (<= 64)
+  // tuning knobs (rgf_set_tuning / rgf_autotune); knob_gen counts changes so
+  // that a batch graph captured with older knobs is captured again
+  int nb = 32;               // leaf width of the panel Cholesky (16, 32 or 64)
+  double split_bias = 1.0;   // the estimated split-product time is scaled by it
+  double tuned_ms = 0.0;     // factorize + RGFdiag time measured by the autotuner
+  long long knob_gen = 0;
 
   // kernel timer: per class (1 = FP64 DMMA GEMM, 2 = split tensor-core GEMM)
   struct TimedLaunch {
@@ -214,7 +222,7 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
                            (g.m + (same ? 0.0 : g.n)) * kq * 8.0 * g.batch / 3e12;
     const double t_split = 50e-6 + t_slice + waves * pairs * (kq / 16.0) * 100e-9;
     const double t_fp64 = 9e-6 + gemm_flops(g) / 0.9e12;
-    split = t_split < t_fp64;
+    split = t_split * h->split_bias < t_fp64;
   }
   if (split) {
     launched = eng->gemm(g, cur_stream(h), h->d_status, &tflops, slices);
@@ -787,6 +795,25 @@ void release(rgf_handle* h) {
   delete h;
 }
 
+// Discard the captured stage graphs (their kernels were cut with the old
+// knobs) and the results computed so far: the next run of every stage
+// launches directly, the one after captures again.
+int drop_graphs(rgf_handle* h) {
+  RGF_CK(cudaStreamSynchronize(h->stream));
+  RGF_CK(cudaStreamSynchronize(h->side));
+  for (cudaGraphExec_t* g : {&h->g_factor, &h->g_selinv, &h->g_inv}) {
+    if (*g) cudaGraphExecDestroy(*g);
+    *g = nullptr;
+  }
+  for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
+  h->g_solve.clear();
+  h->runs_solve.clear();
+  h->runs_factor = h->runs_selinv = h->runs_inv = 0;
+  h->k_factor = h->k_selinv = h->k_inv = 0;
+  h->factored = h->selinv_done = h->inv_done = false;
+  return RGF_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -1269,7 +1296,16 @@ struct rgf_batch {
   long long k_all = 0;
   long long kernels_total = 0;
   int runs = 0;  // graph-mode runs so far (the first one is not captured)
+  long long knob_sum = 0;  // sum of the instances' knob_gen when g_all was captured
 };
+
+namespace {
+long long batch_knob_sum(const rgf_batch* b) {
+  long long s = 0;
+  for (const rgf_handle* h : b->h) s += h->knob_gen;
+  return s;
+}
+}  // namespace
 
 namespace {
 
@@ -1329,6 +1365,7 @@ int batch_issue(rgf_batch* b, bool capture) {
     return cuda_status(e);
   }
   b->k_all = nk;
+  b->knob_sum = batch_knob_sum(b);
   return RGF_OK;
 }
 
@@ -1391,6 +1428,14 @@ int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag) {
   if (cudaSetDevice(b->device) != cudaSuccess) return RGF_ECUDA;
   int st = RGF_OK;
   if (mode == 0) {
+    if (b->g_all && b->knob_sum != batch_knob_sum(b)) {
+      // an instance's knobs changed since the capture: launch directly once,
+      // then capture again
+      RGF_CK(cudaStreamSynchronize(b->stream));
+      cudaGraphExecDestroy(b->g_all);
+      b->g_all = nullptr;
+      b->runs = 0;
+    }
     if (b->runs++ == 0) {
       if ((st = batch_issue(b, false))) return st;
     } else {
@@ -1427,6 +1472,199 @@ int rgf_batch_run(rgf_batch* b, int mode, double* logdet, double* const* diag) {
 int rgf_batch_kernels(rgf_batch* b, long long* kernels) {
   if (!b || !kernels) return RGF_EINVAL;
   *kernels = b->kernels_total;
+  return RGF_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Tuning knobs and the autotuner.  The knobs change how the factorization and
+// selected inversion are cut into kernels (leaf width, look-ahead stream,
+// split/FP64 routing), never the operation count; the autotuner measures the
+// candidates on the instance itself and caches the choice per class.
+// ============================================================================
+namespace {
+
+bool valid_tuning(const rgf_tuning& t) {
+  return (t.leaf_nb == 16 || t.leaf_nb == 32 || t.leaf_nb == 64) &&
+         (t.lookahead == 0 || t.lookahead == 1) && std::isfinite(t.split_bias) &&
+         t.split_bias >= 1.0 / 16 && t.split_bias <= 16.0;
+}
+
+rgf_tuning knobs_of(const rgf_handle* h) {
+  rgf_tuning t{};
+  t.leaf_nb = h->nb;
+  t.lookahead = h->lookahead ? 1 : 0;
+  t.split_bias = h->split_bias;
+  t.ms = h->tuned_ms;
+  return t;
+}
+
+int set_knobs(rgf_handle* h, const rgf_tuning& t) {
+  const int st = drop_graphs(h);
+  if (st) return st;
+  h->nb = t.leaf_nb;
+  h->lookahead = t.lookahead != 0;
+  h->split_bias = t.split_bias;
+  h->tuned_ms = t.ms;
+  h->knob_gen++;
+  return RGF_OK;
+}
+
+// Wall time of one factorize + selected inversion under the handle's current
+// knobs as a steady-state caller sees it: one direct run and one run that
+// captures the stage graphs (both untimed), then the best of `reps` graph
+// replays.  Every stage ends with a synchronisation, so the host clock
+// brackets the device work.
+int time_factor_selinv(rgf_handle* h, int reps, double* ms) {
+  double best = 1e300;
+  for (int r = 0; r < 2 + reps; ++r) {
+    h->factored = false;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int st = ensure_selinv(h);
+    if (st) return st;
+    const double t =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (r >= 2) best = std::min(best, t);
+  }
+  *ms = best;
+  return RGF_OK;
+}
+
+// Coordinate descent from the current knobs: leaf width, then look-ahead,
+// then (split precision) the routing bias.  A candidate replaces the best so
+// far only when it is at least 2% faster, so timing noise does not move the
+// choice away from the defaults.
+int tune_handle(rgf_handle* h, rgf_tuning* out) {
+  rgf_tuning best = knobs_of(h);
+  int st = set_knobs(h, best);
+  if (st) return st;
+  if ((st = time_factor_selinv(h, 2, &best.ms))) return st;
+  auto trial = [&](rgf_tuning t) -> int {
+    if (t.leaf_nb == best.leaf_nb && t.lookahead == best.lookahead &&
+        t.split_bias == best.split_bias)
+      return RGF_OK;
+    int e = set_knobs(h, t);
+    if (e) return e;
+    if ((e = time_factor_selinv(h, 2, &t.ms))) return e;
+    if (t.ms < 0.98 * best.ms) best = t;
+    return RGF_OK;
+  };
+  for (int nb : {16, 32, 64}) {
+    rgf_tuning t = best;
+    t.leaf_nb = nb;
+    if ((st = trial(t))) return st;
+  }
+  {
+    rgf_tuning t = best;
+    t.lookahead = !best.lookahead;
+    if ((st = trial(t))) return st;
+  }
+  if (h->split) {
+    for (double bias : {0.5, 2.0}) {
+      rgf_tuning t = best;
+      t.split_bias = bias;
+      if ((st = trial(t))) return st;
+    }
+  }
+  if ((st = set_knobs(h, best))) return st;
+  *out = best;
+  return RGF_OK;
+}
+
+// Process-wide choices, keyed by everything that changes what is timed.
+struct TuneKey {
+  int device;
+  long long ns, nd;
+  int precision, slices, fp64_diag, selinv_mode, use_graphs;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(device, ns, nd, precision, slices, fp64_diag, selinv_mode, use_graphs) <
+           std::tie(o.device, o.ns, o.nd, o.precision, o.slices, o.fp64_diag, o.selinv_mode,
+                    o.use_graphs);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, rgf_tuning> g_tune_cache;
+
+TuneKey tune_key(const rgf_handle* h) {
+  const rgf_opts& o = h->opts;
+  return {h->device, h->sh.ns, h->sh.nd, o.precision, o.slices, o.fp64_diag, o.selinv_mode,
+          o.use_graphs};
+}
+
+}  // namespace
+
+extern "C" {
+
+int rgf_get_tuning(rgf_handle* h, rgf_tuning* t) {
+  if (!h || !t) return RGF_EINVAL;
+  *t = knobs_of(h);
+  return RGF_OK;
+}
+
+int rgf_set_tuning(rgf_handle* h, const rgf_tuning* t) {
+  if (!h || !t || !valid_tuning(*t)) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  rgf_tuning k = *t;
+  k.ms = 0.0;
+  return set_knobs(h, k);
+}
+
+int rgf_autotune(rgf_handle* h, int flags, rgf_tuning* chosen) {
+  if (!h || (flags & ~RGF_TUNE_FORCE) || h->timer_on) return RGF_EINVAL;
+  if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
+  const TuneKey key = tune_key(h);
+  rgf_tuning t{};
+  bool cached = false;
+  if (!(flags & RGF_TUNE_FORCE)) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      t = it->second;
+      cached = true;
+    }
+  }
+  int st;
+  if (cached) {
+    st = set_knobs(h, t);
+  } else {
+    const rgf_tuning orig = knobs_of(h);
+    st = tune_handle(h, &t);
+    if (st) {
+      set_knobs(h, orig);  // a failed run leaves the knobs as they were
+      return st;
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = t;
+  }
+  if (st) return st;
+  if (chosen) *chosen = t;
+  return RGF_OK;
+}
+
+int rgf_batch_autotune(rgf_batch* b, int flags, size_t* classes) {
+  if (!b || (flags & ~RGF_TUNE_FORCE)) return RGF_EINVAL;
+  if (cudaSetDevice(b->device) != cudaSuccess) return RGF_ECUDA;
+  RGF_CK(cudaStreamSynchronize(b->stream));
+  std::map<std::pair<long long, long long>, std::vector<size_t>> groups;
+  for (size_t i = 0; i < b->h.size(); ++i) groups[{b->h[i]->sh.ns, b->h[i]->sh.nd}].push_back(i);
+  for (auto& kv : groups) {
+    std::vector<size_t> idx = kv.second;
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](size_t x, size_t y) { return b->h[x]->sh.nt < b->h[y]->sh.nt; });
+    rgf_handle* rep = b->h[idx[idx.size() / 2]];
+    rgf_tuning t{};
+    int st = rgf_autotune(rep, flags, &t);
+    if (st) return st;
+    for (size_t i : idx)
+      if (b->h[i] != rep && (st = set_knobs(b->h[i], t))) return st;
+  }
+  if (b->g_all) {
+    cudaGraphExecDestroy(b->g_all);
+    b->g_all = nullptr;
+  }
+  b->runs = 0;
+  if (classes) *classes = groups.size();
   return RGF_OK;
 }
 

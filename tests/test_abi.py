@@ -78,3 +78,50 @@ def test_flop_contract():
     assert abs(f["selinv"] - 5.049e12) / 5.049e12 < 1e-3
     f = algorithmic_flops(1000, 50, 4)
     assert abs(f["total"] - 4.292e11) / 4.292e11 < 1e-3
+
+
+def test_tuning_entry_points_reject_null_handles():
+    import ctypes
+    import rgf_gb300
+    lib = rgf_gb300.load_library()
+    t = rgf_gb300._Tuning()
+    n = ctypes.c_size_t()
+    assert lib.rgf_get_tuning(None, ctypes.byref(t)) == 1
+    assert lib.rgf_set_tuning(None, ctypes.byref(t)) == 1
+    assert lib.rgf_autotune(None, 0, None) == 1
+    assert lib.rgf_batch_autotune(None, 0, ctypes.byref(n)) == 1
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every struct the Python mirror passes through the C ABI has the size
+    and field offsets the C compiler gives it."""
+    import ctypes
+    import shutil
+    import subprocess
+    import rgf_gb300
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not present")
+    structs = {"rgf_opts": rgf_gb300._Opts, "rgf_info_t": rgf_gb300._Info,
+               "rgf_request": rgf_gb300._Request, "rgf_server_stats_t": rgf_gb300._ServerStats,
+               "rgf_tuning": rgf_gb300._Tuning}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rgf.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for ln in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n"):
+        if ln:
+            c, f, v = ln.split()
+            got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
