@@ -179,6 +179,53 @@ def cpu_port_sample(w, target_s: float = 12.0):
     return fl / dt / 1e12, cores, sample, dt
 
 
+def blas_threads():
+    """Threads host LAPACK/BLAS uses for the oracle (threadpoolctl where it is
+    installed, else OPENBLAS_NUM_THREADS, else OpenBLAS's default of all cores)."""
+    try:
+        from threadpoolctl import threadpool_info
+        n = [i["num_threads"] for i in threadpool_info() if i.get("user_api") == "blas"]
+        if n:
+            return max(n), "threadpoolctl"
+    except Exception:
+        pass
+    env = os.environ.get("OPENBLAS_NUM_THREADS") or os.environ.get("OMP_NUM_THREADS")
+    if env and env.isdigit():
+        return int(env), "OPENBLAS_NUM_THREADS"
+    return os.cpu_count(), "OpenBLAS default (all cores)"
+
+
+def cpu_oracle_full(w, ia, ja, a, rhs=None):
+    """The oracle's block recursion (numpy/scipy, host LAPACK on all threads)
+    on the WHOLE workload: ingest + factorize + logDet + exact RGFdiag timed
+    (the CPU baseline), then, untimed, the solve of `rhs`.  Returns the
+    baseline entry and the oracle's results (logdet, diag, x)."""
+    from oracle import rgf_oracle as O
+    from rgf_gb300.flops import algorithmic_flops
+    ns, nt, nd = w["ns"], w["nt"], w["nd"]
+    L = O.Layout(ns, nt, nd)
+    t0 = time.perf_counter()
+    MF = O.ingest(L, ia, ja, a)
+    O.factorize(L, MF)
+    ld = O.logdet(L, MF)
+    diag = O.selinv_exact(L, MF)
+    dt = time.perf_counter() - t0
+    x = O.solve(L, MF, rhs) if rhs is not None else None
+    del MF
+    threads, how = blas_threads()
+    cpu = {"value": algorithmic_flops(ns, nt, nd)["total"] / dt / 1e12, "unit": "TFLOP/s",
+           "cores": threads, "kind": "port",
+           "sample": f"the whole workload (ns={ns}, nt={nt}, nd={nd}): ingest + factorize + "
+                     f"logDet + exact RGFdiag, once",
+           "seconds": dt, "blas_threads": threads, "blas_threads_from": how}
+    return cpu, {"logdet": ld, "diag": diag, "x": x}
+
+
+def rel_errors(ld, diag, ref):
+    return {"logdet_rel": abs(ld - ref["logdet"]) / abs(ref["logdet"]),
+            "diag_max_rel": float(np.max(np.abs(diag - ref["diag"]) / np.abs(ref["diag"])))}
+
+
 def run_reference(args, w):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -195,7 +242,8 @@ def run_reference(args, w):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": args.workload, **cfg_of(w)},
             "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "blas_threads": blas_threads()[0],
+                             "blas_threads_from": blas_threads()[1]},
             "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -430,6 +478,47 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_gemm(args):
+    """One shape of the device GEMM entry point (rgf_dgemm_device):
+    C := -A op(A|B) + C on device buffers, --gemm-reps calls after --warmup,
+    timed with CUDA events on the stream the library launches on.  --syrk
+    makes the product A A^T (the Schur-update shape of the factorization).
+    This is the command the GEMM kernel profiles are taken with; every call
+    also creates and frees the split engine, as the entry point does."""
+    import torch
+    import rgf_gb300
+    m, k = args.m, args.k
+    n = m if args.syrk else args.n
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device="cpu").manual_seed(1)
+    A = torch.randn(k, m, dtype=torch.float64, generator=g).to(dev)      # column-major m x k
+    B = A if args.syrk else torch.randn(k, n, dtype=torch.float64, generator=g).to(dev)
+    C = torch.randn(n, m, dtype=torch.float64, generator=g).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def call():
+        rgf_gb300.dgemm_device(args.precision, "N", "T", m, n, k, -1.0, A.data_ptr(), m,
+                               B.data_ptr(), n, 1.0, C.data_ptr(), m,
+                               stream=stream.cuda_stream, slices=args.slices)
+
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.gemm_reps):
+        call()
+    e1.record(stream)
+    e1.synchronize()
+    us = e0.elapsed_time(e1) * 1e3 / args.gemm_reps
+    flops = 2.0 * m * n * k
+    print(json.dumps({"workload": "gemm", "m": m, "n": n, "k": k, "precision": args.precision,
+                      "slices": args.slices or None, "syrk": args.syrk, "us_per_call": us,
+                      "fp64_equiv_tflops": flops / (us * 1e-6) / 1e12,
+                      "finite": bool(torch.isfinite(C).all().item())}), flush=True)
+
+
 def cfg_of(w):
     return {"ns": w["ns"], "nt": w["nt"], "nd": w["nd"], "seed": w["seed"],
             "spde_grid": w["spde"], "parallelism": "replicas"}
@@ -529,7 +618,9 @@ def run_rgf(args, w):
 
     # 8-RHS solve on the resident factor (refined in FP64 in split precision):
     # time per call (host arrays in and out) and the worst normalized residual
+    d_main = s.RGFdiag()  # the timed steps' diagonal, to host (oracle comparison)
     solve_info = None
+    bsol = xsol = None
     if not args.no_solve:
         from rgf_gb300 import gen as _gen
         bsol = _gen.random_rhs(n, 8, w["seed"])
@@ -562,7 +653,7 @@ def run_rgf(args, w):
                     "achieved": ach, "peak": peaks["bf16_sustained"], "unit": "TFLOP/s",
                     "frac": ach / peaks["bf16_sustained"],
                     # dram read + write of one 2000x2000x2000 launch (ncu --set full,
-                    # python -m rgf_gb300.gemm_bench --m 2000 --k 2000 --syrk); operands
+                    # python bench.py --workload gemm --m 2000 --k 2000 --syrk); operands
                     # are read about once, the slices stay in L2
                     "traffic": 81.6e6, "traffic_unit": "bytes per 2000^3 launch",
                     "peak_source": f"bf16 sustained, {src}",
@@ -579,33 +670,70 @@ def run_rgf(args, w):
                     "kernel_share_of_step": fp["ms"] / ms_step}
     roofline["kernels"] = kernels
 
-    # plain FP64 on the same matrix for comparison (speed-up and accuracy)
-    plain = None
-    if args.precision == "split" and not args.no_fp64_ref:
-        s.close()
-        f = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision="fp64", device=dev)
-        f.factorize(); f.logDet(); d64 = f.RGFdiag()
+    # the same matrix in plain FP64, and in split precision with native-FP64
+    # diagonal blocks, for comparison (speed-up and accuracy); each handle
+    # runs two untimed steps (direct launch, graph capture), then one timed
+    mf_bytes = s.info()["mf_size"] * 8
+    s.close()
+
+    def variant(precision, fp64_diag=1):
+        f = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=precision, slices=args.slices,
+                          device=dev, fp64_diag=fp64_diag)
+        for _ in range(2):
+            f.factorize(); f.logDet(); f.diag_device_ptr()
         fs = torch.cuda.ExternalStream(f.stream())
         torch.cuda.synchronize()
         p0 = torch.cuda.Event(enable_timing=True); p1 = torch.cuda.Event(enable_timing=True)
         p0.record(fs)
-        f.factorize(); ld64 = f.logDet(); f.diag_device_ptr()
+        f.factorize(); ld = f.logDet(); f.diag_device_ptr()
         p1.record(fs); p1.synchronize()
         pms = p0.elapsed_time(p1)
+        d = f.RGFdiag()
         f.close()
-        s = rgf_gb300.RGF(ia_p, ja_p, a_p, ns, nt, nd, precision=args.precision,
-                          slices=args.slices, device=dev, fp64_diag=not args.no_fp64_diag)
-        dsp = s.RGFdiag()
-        plain = {"value": flops / (pms * 1e-3) / 1e12, "ms_per_step": pms, "steps": 1, "warmup": 1,
+        return pms, ld, d
+
+    plain = native_diag = None
+    ld64 = d64 = ldn = dn = None
+    if args.precision == "split" and not args.no_fp64_ref:
+        pms, ld64, d64 = variant("fp64")
+        plain = {"value": flops / (pms * 1e-3) / 1e12, "ms_per_step": pms, "steps": 1, "warmup": 2,
                  "speedup_of_split": pms / ms_step,
                  "split_vs_fp64": {"logdet_rel": abs(logdet - ld64) / abs(ld64),
-                                   "diag_max_rel": float(np.max(np.abs(dsp - d64) / np.abs(d64)))}}
+                                   "diag_max_rel": float(np.max(np.abs(d_main - d64) / np.abs(d64)))}}
+        if not args.no_fp64_diag:
+            nms, ldn, dn = variant("split", fp64_diag="native")
+            native_diag = {"value": flops / (nms * 1e-3) / 1e12, "ms_per_step": nms, "steps": 1,
+                           "warmup": 2, "diag_products": "native FP64 (DMMA)",
+                           "vs_fp64": {"logdet_rel": abs(ldn - ld64) / abs(ld64),
+                                       "diag_max_rel": float(np.max(np.abs(dn - d64) / np.abs(d64)))}}
 
+    # the oracle on the whole workload: CPU baseline and parity of every GPU result
     cpu = None
+    oracle_err = None
     if rank == 0 and not args.no_cpu:
-        tf, cores, sample, dt = cpu_port_sample(w, target_s=args.ref_seconds)
-        cpu = {"value": tf, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-               "sample": sample, "seconds": dt}
+        if args.cpu_prefix:
+            tf, cores, sample, dt = cpu_port_sample(w, target_s=args.ref_seconds)
+            cpu = {"value": tf, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                   "sample": sample, "seconds": dt}
+        else:
+            cpu, ref = cpu_oracle_full(w, ia_p, ja_p, a_p, bsol)
+            oracle_err = {args.precision: rel_errors(logdet, d_main, ref),
+                          "gates": {"fp64": {"logdet_rel": 1e-12, "diag_max_rel": 1e-10},
+                                    "split": {"logdet_rel": 1e-9, "diag_max_rel": 1e-8}}}
+            if plain is not None:
+                oracle_err["fp64"] = rel_errors(ld64, d64, ref)
+            if native_diag is not None:
+                oracle_err["split_native_fp64_diag"] = rel_errors(ldn, dn, ref)
+            if bsol is not None and ref["x"] is not None:
+                oracle_err["solve_8rhs"] = {
+                    "x_max_rel": float(np.max(np.abs(xsol - ref["x"])) / np.max(np.abs(ref["x"]))),
+                    "max_residual_normalized": solve_info["max_residual_normalized"]}
+    if args.precision == "fp64":
+        diag_label = "FP64 (DMMA)"
+    elif args.no_fp64_diag:
+        diag_label = "split-%d (bulk slice count)" % (args.slices or 5)
+    else:
+        diag_label = "split-7 (55-bit operands: FP64-accurate emulation on the tensor cores)"
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -613,20 +741,21 @@ def run_rgf(args, w):
                 "dtype": "f64" if args.precision == "fp64" else "bf16-slices/f64",
                 "data": "synthetic",
                 "config": {"workload": args.workload, **cfg_of(w), "precision": args.precision,
-                           "fp64_diag": not args.no_fp64_diag, "slices": args.slices or 5, "slice_bits": 8 * (args.slices or 5) - 1,
+                           "slices": args.slices or 5, "slice_bits": 8 * (args.slices or 5) - 1,
+                           "diag_products": diag_label,
                            "l2": "inputs larger than L2 (CSC %.1f GB, factor %.1f GB)" % (
-                               h2d / 1e9, s.info()["mf_size"] * 8 / 1e9)},
+                               h2d / 1e9, mf_bytes / 1e9)},
                 "e2e": ({"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
                          "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "parts": e2e_parts} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
-                "plain_fp64": plain, "solve": solve_info,
+                "plain_fp64": plain, "split_native_fp64_diag": native_diag,
+                "solve": solve_info, "oracle_err": oracle_err,
                 "clocks": clk, "logdet": logdet,
                 "timed_region": "each stage replayed as one CUDA graph; kernel classes timed "
                                 "on one extra step with events around every GEMM, each run "
                                 "alone (serialised)"}
         print(json.dumps(line), flush=True)
-    s.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -638,7 +767,7 @@ def main():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["rgf", "reference"], default="rgf")
-    p.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "serve"],
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch", "serve", "gemm"],
                    default="ns2000_nt100_nd6")
     p.add_argument("--rate", type=float, default=2000.0)
     p.add_argument("--serve-requests", type=int, default=400)
@@ -663,7 +792,23 @@ def main():
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--ref-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-prefix", action="store_true",
+                   help="time the oracle on a prefix of the block columns (about "
+                        "--ref-seconds) instead of the whole workload; no oracle errors")
+    # --workload gemm: one product shape through rgf_dgemm_device
+    p.add_argument("--m", type=int, default=2000)
+    p.add_argument("--n", type=int, default=2000)
+    p.add_argument("--k", type=int, default=2000)
+    p.add_argument("--syrk", action="store_true", help="gemm workload: B = A (product A A^T)")
+    p.add_argument("--gemm-reps", type=int, default=10)
     args = p.parse_args()
+    if args.workload == "gemm":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the gemm workload times one "
+                              "product of this library's kernels; the reference has none"}))
+        else:
+            run_gemm(args)
+        return
     if args.workload == "serve":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no request "

@@ -184,6 +184,21 @@ int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m,
                      double alpha, const double* A, int lda, const double* B, int ldb,
                      double beta, double* C, int ldc, void* stream);
 
+/* Failure handling.  Every device-side wait is bounded; a wait that runs out
+ * makes the stage return RGF_ETIMEOUT and leaves the handle usable (the next
+ * call recomputes).  rgf_set_wait_limit sets how many times the leaf
+ * Cholesky's wait for the previous column's pivot polls before it gives up
+ * (0 = the default, 2^26 polls); a small limit makes that wait run out, which
+ * is how the timeout path is tested.  Changing it drops the handle's captured
+ * stage graphs and its results. */
+int rgf_set_wait_limit(rgf_handle* h, int polls);
+
+/* Failure injection for tests, process-wide: the next `after` device
+ * allocations of the library succeed, the one after that fails as if the
+ * device were out of memory (the call returns RGF_ENOMEM), and later ones
+ * succeed again.  after < 0 switches it off. */
+int rgf_debug_fail_alloc_after(long long after);
+
 /* Measured FP64 (DMMA m8n8k4) throughput of the current device in TFLOP/s:
  * the denominator of the FP64 roofline.  Runs about 100 ms of GPU work. */
 int rgf_measure_fp64_peak(double* tflops);
@@ -204,11 +219,21 @@ int rgf_measure_fp64_peak(double* tflops);
  * embeddings that forbid hidden allocations.  It allocates nothing: its
  * scratch (n doubles) is a fixed 8 MiB device array that every GPU loading
  * this library holds until the process exits, so n must not exceed
- * RGF_NOALLOC_MAX_N (RGF_EINVAL otherwise).  The first call on a device looks
- * up that array's device address (once per device, with the device current);
- * make that first call before any stream capture.  All calls share the array:
- * calls whose work overlaps on the GPU race and give wrong results, so
- * serialize them (one stream, or events). */
+ * RGF_NOALLOC_MAX_N (RGF_EINVAL otherwise).
+ * The array belongs to this library's device code, which CUDA loads on a
+ * device at the first call there (lazy module loading): that first call
+ * reserves the 8 MiB and should be made during set-up, before the caller's
+ * allocator takes the rest of the memory and before any stream capture.
+ * Later calls reserve nothing.  Each call looks up the array's device
+ * address in the current context.
+ * The CSC must be a valid lower CSC (d_ia non-decreasing from 0, every row
+ * index in [c, n) for column c), for example one that rgf_create accepted.
+ * Row indices outside that range are skipped, never written through, and
+ * make both outputs NaN; d_ia itself is not checked.
+ * An error already pending on the calling thread is reported as RGF_ECUDA
+ * and left pending.  All calls share the array: calls whose work overlaps on
+ * the GPU race and give wrong results, so serialize them (one stream, or
+ * events). */
 int rgf_residual_norm_noalloc(size_t n, const size_t* d_ia, const size_t* d_ja,
                               const double* d_a, const double* d_x, const double* d_b,
                               double* d_out, void* stream);

@@ -3,9 +3,10 @@
 Compiles the reference's unmodified RGF.H (through replay_driver.C) and its
 unmodified main.C + Utilities.C against the host stand-ins in this folder
 (MAGMA v2 subset, Fortran BLAS subset, CWC_utility entry points).  Needs the
-reference tree (default /root/reference, or $RGF_REFERENCE) and g++; outputs
-go only to oracle/_ref/.  Test infrastructure: used to generate the golden
-vectors in tests/golden/.
+reference tree and g++; outputs go only to oracle/_ref/.  This recipe is the
+one place that locates the reference tree: $RGF_REFERENCE when set, else the
+development machine's mount point (reference_root()).  Test infrastructure:
+used to generate the golden vectors in tests/golden/.
 """
 import os
 import shutil
@@ -14,8 +15,15 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-REF = os.environ.get("RGF_REFERENCE", "/root/reference")
 CUDA_INC = "/usr/local/cuda/include"
+
+
+def reference_root() -> str:
+    """The reference tree: $RGF_REFERENCE, else the development machine's mount."""
+    return os.environ.get("RGF_REFERENCE", "/root/reference")
+
+
+REF = reference_root()
 
 
 def build() -> dict:

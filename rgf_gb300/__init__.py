@@ -137,6 +137,9 @@ _SIGS = {
     "rgf_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(_Tuning)]),
     "rgf_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_Tuning)]),
     "rgf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
+    "rgf_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
+    "rgf_debug_fail_alloc_after": (C.c_int, [C.c_longlong]),
+    "rgf_residual_norm_noalloc": (C.c_int, [C.c_size_t] + [C.c_void_p] * 7),
 }
 
 
@@ -178,6 +181,12 @@ def hermitian_embed(ia, ja, a, ns: int, nt: int, nd: int):
     _check(lib.rgf_hermitian_embed(_ptr(ia), _ptr(ja), _ptr(a), ns, nt, nd, _ptr(ia2), _ptr(ja2),
                                    _ptr(a2), C.byref(nnz2)), "rgf_hermitian_embed")
     return ia2, ja2, a2
+
+
+def debug_fail_alloc_after(after: int) -> None:
+    """Failure injection for tests: the next ``after`` device allocations of
+    the library succeed and the one after fails (RGF_ENOMEM); -1 turns it off."""
+    _check(load_library().rgf_debug_fail_alloc_after(int(after)), "rgf_debug_fail_alloc_after")
 
 
 def measure_fp64_peak() -> float:
@@ -360,6 +369,11 @@ class RGF:
         _check(self._lib.rgf_autotune(self._h, TUNE_FORCE if force else 0, C.byref(t)),
                "rgf_autotune")
         return _tuning_dict(t)
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Poll limit of the leaf Cholesky's pivot wait (0 = default); a wait
+        that runs out makes the stage raise RGFError(RGF_ETIMEOUT)."""
+        _check(self._lib.rgf_set_wait_limit(self._h, int(polls)), "rgf_set_wait_limit")
 
     def kernel_timer(self, enable) -> None:
         """True/1: time bulk GEMMs; 2: also print per-shape totals on reset."""

@@ -260,7 +260,8 @@ __device__ __forceinline__ int ld_acquire_cta(const int* p) {
 }
 
 __global__ void __launch_bounds__(256) leaf_potrf_flow_kernel(double* T, long long ldt, int nbk,
-                                                              int col0, DevStatus* st) {
+                                                              int col0, DevStatus* st,
+                                                              int wait_polls) {
   __shared__ double S[64][65];
   __shared__ double ys[64];
   __shared__ int ready;   // y_0 .. y_ready are published
@@ -284,10 +285,11 @@ __global__ void __launch_bounds__(256) leaf_potrf_flow_kernel(double* T, long lo
   }
   for (int j = 0; j + 1 < nbk; ++j) {
     if (ld_acquire_cta(&ready) < j) {
+      // bounded: after wait_polls polls the leaf gives up and records a timeout
       int it = 0;
-      while (ld_acquire_cta(&ready) < j && !abort_ && ++it < (1 << 26)) {
+      while (ld_acquire_cta(&ready) < j && !abort_ && ++it < wait_polls) {
       }
-      if (it >= (1 << 26)) {
+      if (it >= wait_polls) {
         abort_ = 1;
         if (lane == 0) atomicExch(&st->timeout, 1);
       }
@@ -595,9 +597,10 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
 }
 
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* st,
-                       cudaStream_t s) {
+                       cudaStream_t s, int wait_polls) {
   if (nbk <= 0) return;
-  leaf_potrf_flow_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, st);
+  leaf_potrf_flow_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, st,
+                                           wait_polls > 0 ? wait_polls : LEAF_WAIT_POLLS);
 }
 
 void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,

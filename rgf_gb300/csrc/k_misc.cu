@@ -139,16 +139,25 @@ __global__ void copy_kernel(const double* X, long long ldx, double* Y, long long
 
 // y = A x with A symmetric, stored as its lower CSC: column c contributes
 // a_rc x_c to y_r (scatter) and, off the diagonal, a_rc x_r to y_c (gather).
+// Entries outside the lower triangle (r < c) or past the last row (r >= n)
+// are skipped, so every write stays inside y[0, n); when `bad` is given such
+// an entry also sets *bad.
 __global__ void sym_spmv_kernel(long long n, const size_t* __restrict__ ia,
                                 const size_t* __restrict__ ja, const double* __restrict__ a,
-                                const double* __restrict__ x, double* y) {
+                                const double* __restrict__ x, double* y, int* bad) {
   const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= n) return;
   const double xc = x[c];
   double g = 0.0;
+  bool skipped = false;
   for (size_t e = ia[c] + lane; e < ia[c + 1]; e += 32) {
-    const long long r = (long long)ja[e];
+    const size_t ru = ja[e];
+    if (ru < (size_t)c || ru >= (size_t)n) {
+      skipped = true;
+      continue;
+    }
+    const long long r = (long long)ru;
     const double v = a[e];
     atomicAdd(&y[r], v * xc);
     if (r != c) g += v * x[r];
@@ -156,29 +165,66 @@ __global__ void sym_spmv_kernel(long long n, const size_t* __restrict__ ia,
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
   if (lane == 0 && g != 0.0) atomicAdd(&y[c], g);
+  if (skipped && bad) atomicExch(bad, 1);
 }
 
-__global__ void residual_norm_kernel(long long n, const double* b, const double* y, double* out) {
+// out[0] = ||b - y||_2, out[1] = ||b||_2 (one CTA, 1024 threads).  As in
+// dnrm2, the sums of squares are scaled so that neither overflows nor
+// underflows: a first pass finds max |b - y| and max |b| (order-independent),
+// a second sums the squares of the entries scaled by the power of two just
+// above each maximum (exact scaling), in a fixed tree order.  If *bad is set
+// (an index was out of range in the product) both outputs are NaN.
+__device__ __forceinline__ double pow2_below_inv(double mx) {
+  // 2^-e with 2^(e-1) <= mx < 2^e (mx > 0 and finite), so mx * 2^-e is in [0.5, 1)
+  int e = 0;
+  frexp(mx, &e);
+  return ldexp(1.0, -e);
+}
+
+__global__ void residual_norm_kernel(long long n, const double* b, const double* y, double* out,
+                                     const int* bad) {
   __shared__ double s1[1024], s2[1024];
-  double r2 = 0.0, b2 = 0.0;
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-    const double r = b[i] - y[i];
-    r2 += r * r;
-    b2 += b[i] * b[i];
+  const int t = threadIdx.x;
+  double m1 = 0.0, m2 = 0.0;
+  for (long long i = t; i < n; i += blockDim.x) {
+    m1 = fmax(m1, fabs(b[i] - y[i]));
+    m2 = fmax(m2, fabs(b[i]));
   }
-  s1[threadIdx.x] = r2;
-  s2[threadIdx.x] = b2;
+  s1[t] = m1;
+  s2[t] = m2;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      s1[threadIdx.x] += s1[threadIdx.x + w];
-      s2[threadIdx.x] += s2[threadIdx.x + w];
+    if (t < w) {
+      s1[t] = fmax(s1[t], s1[t + w]);
+      s2[t] = fmax(s2[t], s2[t + w]);
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    out[0] = sqrt(s1[0]);
-    out[1] = sqrt(s2[0]);
+  const double mr = s1[0], mb = s2[0];
+  __syncthreads();
+  const bool fr = mr > 0.0 && isfinite(mr), fb = mb > 0.0 && isfinite(mb);
+  const double sr = fr ? pow2_below_inv(mr) : 1.0, sb = fb ? pow2_below_inv(mb) : 1.0;
+  double r2 = 0.0, b2 = 0.0;
+  for (long long i = t; i < n; i += blockDim.x) {
+    const double r = (b[i] - y[i]) * sr, bb = b[i] * sb;
+    r2 += r * r;
+    b2 += bb * bb;
+  }
+  s1[t] = r2;
+  s2[t] = b2;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      s1[t] += s1[t + w];
+      s2[t] += s2[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    const bool invalid = bad && *bad;
+    out[0] = invalid ? nan : (fr ? sqrt(s1[0]) / sr : mr);
+    out[1] = invalid ? nan : (fb ? sqrt(s2[0]) / sb : mb);
   }
 }
 
@@ -266,7 +312,7 @@ void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size
   const long long threads = n * 32;
   for (int q = 0; q < nrhs; ++q)
     sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, X + q * n,
-                                                                      Y + q * n);
+                                                                      Y + q * n, nullptr);
   const long long len = n * nrhs;
   sub_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, B, Y, R);
 }
@@ -275,13 +321,16 @@ void launch_add(long long len, double* x, const double* d, cudaStream_t s) {
   add_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, x, d);
 }
 
-void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
-                     const double* x, const double* b, double* scratch, double* out,
-                     cudaStream_t s) {
-  cudaMemsetAsync(scratch, 0, sizeof(double) * n, s);
+cudaError_t launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
+                            const double* x, const double* b, double* scratch, double* out,
+                            int* bad, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(double) * n, s);
+  if (e == cudaSuccess && bad) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
   const long long threads = n * 32;
-  sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, scratch);
-  residual_norm_kernel<<<1, 1024, 0, s>>>(n, b, scratch, out);
+  sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, scratch, bad);
+  residual_norm_kernel<<<1, 1024, 0, s>>>(n, b, scratch, out, bad);
+  return cudaGetLastError();
 }
 
 void launch_arrow_gemv(const BtaShape& sh, const double* MF, const double* rhs, long long ldr,

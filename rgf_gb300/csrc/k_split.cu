@@ -31,10 +31,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "../../include/rgf.h"
 #include "rgf_split.h"
@@ -44,27 +47,34 @@ namespace rgf {
 namespace {
 
 constexpr int BM = 128, BN = 128, BKE = 64;  // tile rows, cols, K elements per swizzle atom
-constexpr int ATOMS = 2;                      // atoms per pipeline stage
-constexpr int SBK = BKE * ATOMS;              // K terms per stage
-constexpr int NSTAGE = 3;
+constexpr int SBK = BKE;                      // K terms per pipeline stage (one atom)
+constexpr int NSTAGE = 4;
 constexpr int SPLIT_BETA = 8;
 // terms per exact FP32 sum: 2^24 / 2^(2 beta - 2) (balanced digits, products <= 2^14)
 constexpr int EXACT_TERMS = 1 << (24 - 2 * SPLIT_BETA + 2);
-constexpr int MAXPAIRS = 45;
-constexpr int MAXGROUPS = 48;
+constexpr int MAXSLOTS = 24;
+constexpr int MAXGROUPS = 32;
 constexpr int NUM_THREADS = 320;              // warp 0 TMA, warp 1 MMA, warps 2..9 drain
-constexpr uint32_t TILE_BYTES = BM * BKE * 2; // 16 KiB per operand tile
+constexpr uint32_t TILE_BYTES = BM * BKE * 2; // 16 KiB per operand tile (128 rows x 64 terms)
+constexpr uint32_t TMEM_COLS = 512;           // two accumulators of 2 x 128 columns
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any mbarrier wait
+constexpr unsigned char NO_SLICE = 0xFF;
 
+// A slot is one MMA stream: digit slice s of op(A) against one or two digit
+// slices of op(B) stacked along N (t1 in accumulator columns 0..127, t2 in
+// 128..255), i.e. the products A_s B_t1 and A_s B_t2 of one N=256 MMA.  A
+// group holds slots whose products share their levels (s + t1 = l1 for the
+// first half, s + t2 = l2 for the second), so each half of the accumulator
+// sums one level exactly.
 struct SplitParams {
   int m, n, k;
   int S, beta, cs;
-  int npairs;
-  unsigned char ps[MAXPAIRS], pt[MAXPAIRS];
-  // pair groups: pairs g0 .. g0 + gs - 1 (one level, glevel = s + t - 2)
-  // accumulate together over gchunk stages at a time
+  int nslots;
+  unsigned char ss[MAXSLOTS], st1[MAXSLOTS], st2[MAXSLOTS];
+  // groups: slots g0 .. g0 + gs - 1 accumulate together over gchunk stages
+  // at a time; level of the first half gl1, of the second gl2 (NO_SLICE: none)
   int ngroups;
-  unsigned char g0[MAXGROUPS], gs[MAXGROUPS], glevel[MAXGROUPS], gchunk[MAXGROUPS];
+  unsigned char g0[MAXGROUPS], gs[MAXGROUPS], gl1[MAXGROUPS], gl2[MAXGROUPS], gchunk[MAXGROUPS];
   int triA, triB, outLower;
   const int* exA;
   const int* exB;
@@ -116,9 +126,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Bounded wait: gives up after WAIT_NS of wall time (or when another role of
-// the CTA already gave up), raises the CTA abort flag, records a timeout in
-// the device status word and returns false.
+// Bounded wait in the pipeline: gives up after WAIT_NS of wall time (or when
+// another role of the CTA already gave up), raises the CTA abort flag,
+// records a timeout in the device status word and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
                                           DevStatus* st) {
   if (mbar_try_wait(bar, parity)) return true;
@@ -133,6 +143,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   return false;
 }
 
+// Bounded wait for asynchronous work this CTA itself issued (TMA loads,
+// MMAs) before it may release TMEM and exit: it ignores the abort flag, so an
+// aborted CTA still lets its own copies and MMAs land, and gives up only
+// after WAIT_NS (recording a timeout).
+__device__ __forceinline__ void mbar_wait_own(uint64_t* bar, uint32_t parity, DevStatus* st) {
+  if (mbar_try_wait(bar, parity)) return;
+  const unsigned long long t0 = global_ns();
+  for (long long it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return;
+    if ((it & 255) == 0 && global_ns() - t0 > WAIT_NS) break;
+  }
+  atomicExch(&st->timeout, 1);
+}
+
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
                                             int x, int y, int z) {
   asm volatile(
@@ -142,7 +166,8 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
-// K-major operand tile: 128 rows of 128 bytes, 128B swizzle, 8-row groups 1024 B apart.
+// K-major operand: rows of 128 bytes, 128B swizzle, 8-row groups 1024 B apart.
+// Two 128-row tiles stored back to back form one 256-row operand.
 __device__ __forceinline__ uint64_t smem_desc_sw128(const void* base) {
   uint64_t d = 0;
   d |= (uint64_t)((smem_u32(base) >> 4) & 0x3FFF);       // start address
@@ -153,16 +178,20 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(const void* base) {
   return d;
 }
 
-// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M=128, N=128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M=128, N=n.
+constexpr uint32_t idesc_n(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+constexpr uint32_t IDESC_N128 = idesc_n(128);
+constexpr uint32_t IDESC_N256 = idesc_n(256);
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t accumulate) {
+                                          uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
@@ -196,6 +225,13 @@ __device__ __forceinline__ double pow2(int e) {
   return ldexp(1.0, e);
 }
 
+// exact FP32 integer partial v, weighted by 2^sh into the fixed-point sum
+// (a negative sh rounds half up, as a shift of the integer)
+__device__ __forceinline__ long long shifted(uint32_t bits, int sh) {
+  const long long v = (long long)__float2int_rn(__uint_as_float(bits));
+  return sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+}
+
 // Per-tile K range: triangular operands have no terms outside their triangle.
 __device__ __forceinline__ void tile_kblocks(const SplitParams& p, int m0, int n0, int& kb_lo,
                                              int& kb_hi) {
@@ -209,19 +245,22 @@ __device__ __forceinline__ void tile_kblocks(const SplitParams& p, int m0, int n
 }
 
 // ---- the slice-product GEMM ---------------------------------------------------
+// Shared memory: NSTAGE stages, each one 64-term atom of A (16 KiB) and up to
+// two stacked atoms of B (32 KiB), then the barriers.
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                       const __grid_constant__ CUtensorMap tmB, const __grid_constant__ SplitParams p) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
-  uint8_t* tilesA = smem;                                  // NSTAGE x ATOMS x 16 KiB
-  uint8_t* tilesB = smem + NSTAGE * ATOMS * TILE_BYTES;    // NSTAGE x ATOMS x 16 KiB
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 2 * NSTAGE * ATOMS * TILE_BYTES);
+  uint8_t* tilesA = smem;                                  // NSTAGE x 16 KiB
+  uint8_t* tilesB = smem + NSTAGE * TILE_BYTES;            // NSTAGE x 32 KiB
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + 3 * NSTAGE * TILE_BYTES);
   uint64_t* empty = full + NSTAGE;
   uint64_t* acc_full = empty + NSTAGE;                     // 2 accumulators
   uint64_t* acc_empty = acc_full + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  uint64_t* mma_done = acc_empty + 2;                      // every MMA of this CTA retired
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -233,7 +272,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   int kb_lo, kb_hi;
   tile_kblocks(p, m0, n0, kb_lo, kb_hi);
   const int nkb = kb_hi - kb_lo;
-  // jobs: for each pair group, K chunks of gchunk stages
+  // jobs: for each group, K chunks of gchunk stages
   int njobs = 0;
   for (int g = 0; g < p.ngroups; ++g) njobs += nkb > 0 ? (nkb + p.gchunk[g] - 1) / p.gchunk[g] : 0;
 
@@ -246,12 +285,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       mbar_init(&acc_full[b], 1);
       mbar_init(&acc_empty[b], 8);
     }
+    mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {  // allocate 256 TMEM columns (two 128-column accumulators)
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-                     smem_u32(tmem_slot))
+  if (warp == 1) {  // all 512 TMEM columns: two accumulators of 256 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)), "n"(TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -266,29 +306,32 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       long long use = 0;
       bool ok = true;
       for (int g = 0; g < p.ngroups && ok; ++g) {
-        const int chunk = p.gchunk[g], p0 = p.g0[g], p1 = p0 + p.gs[g];
+        const int chunk = p.gchunk[g], q0 = p.g0[g], q1 = q0 + p.gs[g];
         for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk) {
           const int kb1 = min(kb_hi, kb0 + chunk);
-          for (int pr = p0; pr < p1 && ok; ++pr)
+          for (int q = q0; q < q1 && ok; ++q) {
+            const bool two = p.st2[q] != NO_SLICE;
             for (int kb = kb0; kb < kb1; ++kb, ++use) {
               const int s = (int)(use % NSTAGE);
               const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
               if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, p.st)) { ok = false; break; }
-              mbar_expect_tx(&full[s], 2 * ATOMS * TILE_BYTES);
-              for (int at = 0; at < ATOMS; ++at) {  // K beyond the slices' extent reads zeros
-                const int x = kb * SBK + at * BKE;
-                tma_load_3d(tilesA + (s * ATOMS + at) * TILE_BYTES, &tmA, &full[s], x, m0,
-                            zS + p.ps[pr]);
-                tma_load_3d(tilesB + (s * ATOMS + at) * TILE_BYTES, &tmB, &full[s], x, n0,
-                            zS + p.pt[pr]);
-              }
+              mbar_expect_tx(&full[s], (two ? 3 : 2) * TILE_BYTES);
+              const int x = kb * SBK;  // K beyond the slices' extent reads zeros
+              uint8_t* bs = tilesB + s * 2 * TILE_BYTES;
+              tma_load_3d(tilesA + s * TILE_BYTES, &tmA, &full[s], x, m0, zS + p.ss[q]);
+              tma_load_3d(bs, &tmB, &full[s], x, n0, zS + p.st1[q]);
+              if (two) tma_load_3d(bs + TILE_BYTES, &tmB, &full[s], x, n0, zS + p.st2[q]);
             }
+          }
         }
       }
-      // let in-flight loads land before the CTA can exit
-      if (use > 0) {
-        const long long last = use - 1;
-        mbar_wait(&full[last % NSTAGE], (uint32_t)((last / NSTAGE) & 1), abort_flag, p.st);
+      // Every stage with a load issued waits for that load to land (also on
+      // abort), so no copy into this CTA's shared memory is in flight at exit.
+      // Uses of one stage complete in order; only its last use can be open.
+      for (int s = 0; s < NSTAGE; ++s) {
+        if (use <= s) break;
+        const long long last = s + ((use - 1 - s) / NSTAGE) * NSTAGE;
+        mbar_wait_own(&full[s], (uint32_t)((last / NSTAGE) & 1), p.st);
       }
     }
   } else if (warp == 1) {
@@ -298,48 +341,46 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       int j = 0;
       bool ok = true;
       for (int g = 0; g < p.ngroups && ok; ++g) {
-        const int chunk = p.gchunk[g], npr = p.gs[g];
+        const int chunk = p.gchunk[g], q0 = p.g0[g], q1 = q0 + p.gs[g];
         for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk, ++j) {
           const int kb1 = min(kb_hi, kb0 + chunk);
           const int buf = j & 1;
           const uint32_t aph = (uint32_t)((j >> 1) & 1);
           if (!mbar_wait(&acc_empty[buf], aph ^ 1u, abort_flag, p.st)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t tacc = tmem_base + (uint32_t)(buf * BN);
+          const uint32_t tacc = tmem_base + (uint32_t)(buf * 2 * BN);
           bool first = true;
-          for (int pr = 0; pr < npr && ok; ++pr)
+          for (int q = q0; q < q1 && ok; ++q) {
+            const uint32_t idesc = p.st2[q] != NO_SLICE ? IDESC_N256 : IDESC_N128;
             for (int kb = kb0; kb < kb1; ++kb, ++use) {
               const int s = (int)(use % NSTAGE);
               const uint32_t ph = (uint32_t)((use / NSTAGE) & 1);
               if (!mbar_wait(&full[s], ph, abort_flag, p.st)) { ok = false; break; }
               tc_fence_after();
+              const uint64_t ad = smem_desc_sw128(tilesA + s * TILE_BYTES);
+              const uint64_t bd = smem_desc_sw128(tilesB + s * 2 * TILE_BYTES);
 #pragma unroll
-              for (int at = 0; at < ATOMS; ++at) {
-                const uint64_t ad = smem_desc_sw128(tilesA + (s * ATOMS + at) * TILE_BYTES);
-                const uint64_t bd = smem_desc_sw128(tilesB + (s * ATOMS + at) * TILE_BYTES);
-#pragma unroll
-                for (int kk = 0; kk < BKE / 16; ++kk) {  // +32 bytes per K=16 step in the atom
-                  umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2),
-                            first ? 0u : 1u);
-                  first = false;
-                }
+              for (int kk = 0; kk < BKE / 16; ++kk) {  // +32 bytes per K=16 step in the atom
+                umma_bf16(tacc, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2), idesc,
+                          first ? 0u : 1u);
+                first = false;
               }
               umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             }
+          }
           if (!ok) break;
           umma_commit(&acc_full[buf]);  // accumulator ready for the drain warps
         }
       }
-      // wait for the last commit so no MMA is in flight at exit
-      if (njobs > 0 && !*abort_flag) {
-        const int j = njobs - 1;
-        mbar_wait(&acc_full[j & 1], (uint32_t)((j >> 1) & 1), abort_flag, p.st);
-      }
+      // One more commit tracks every MMA this thread issued: wait for it (also
+      // on abort) so that no MMA still writes TMEM when it is released.
+      umma_commit(mma_done);
+      mbar_wait_own(mma_done, 0, p.st);
     }
   } else {
     // ---------------- drain warps (2..9) ----------------
     const int q = warp & 3;            // TMEM lane quadrant this warp may access
-    const int half = (warp - 2) >> 2;  // column half: 0 or 1
+    const int half = (warp - 2) >> 2;  // column half of the output tile: 0 or 1
     const int row = q * 32 + lane;     // accumulator row of this thread
     long long acc[64];
 #pragma unroll
@@ -355,17 +396,24 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const int buf = j & 1;
       if (!mbar_wait(&acc_full[buf], (uint32_t)((j >> 1) & 1), abort_flag, p.st)) break;
       tc_fence_after();
-      const int sh = p.beta * (p.S - 1 - p.glevel[g]) - p.cs;
       const uint32_t taddr =
-          tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + half * 64);
+          tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN + half * 64);
+      const int sh1 = p.beta * (p.S - 1 - p.gl1[g]) - p.cs;
 #pragma unroll
       for (int part = 0; part < 4; ++part) {
         uint32_t r[16];
         tmem_ld16(taddr + part * 16, r);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const long long v = (long long)__float2int_rn(__uint_as_float(r[i]));
-          acc[part * 16 + i] += sh >= 0 ? (v << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+        for (int i = 0; i < 16; ++i) acc[part * 16 + i] += shifted(r[i], sh1);
+      }
+      if (p.gl2[g] != NO_SLICE) {
+        const int sh2 = p.beta * (p.S - 1 - p.gl2[g]) - p.cs;
+#pragma unroll
+        for (int part = 0; part < 4; ++part) {
+          uint32_t r[16];
+          tmem_ld16(taddr + BN + part * 16, r);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) acc[part * 16 + i] += shifted(r[i], sh2);
         }
       }
       tc_fence_before();
@@ -397,7 +445,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem_base)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                 "n"(TMEM_COLS)
                  : "memory");
   }
 }
@@ -660,7 +709,7 @@ bool make_map(CUtensorMap* map, void* base, int S, int Rp, int Kp) {
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-constexpr size_t SMEM_BYTES = 1024 + 2 * NSTAGE * ATOMS * TILE_BYTES + 256;
+constexpr size_t SMEM_BYTES = 1024 + 3 * NSTAGE * TILE_BYTES + 256;
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
@@ -693,7 +742,7 @@ int SplitEngine::ensure_ws(size_t bytes) {
   if (ws_) cudaFree(ws_);
   ws_ = nullptr;
   ws_bytes_ = 0;
-  if (cudaMalloc(&ws_, bytes) != cudaSuccess) {
+  if (device_malloc(&ws_, bytes) != cudaSuccess) {
     cudaGetLastError();
     return RGF_ENOMEM;
   }
@@ -711,6 +760,81 @@ size_t item_bytes(int S, int RpA, int RpB, int Kp) {
          align256((size_t)(RpA + RpB) * sizeof(int)) +
          align256((size_t)(RpA + RpB) * sizeof(unsigned long long));
 }
+
+// ---- slot plan: which digit products share an MMA --------------------------
+// The products A_a B_b (1-based digits a, b <= S, level a + b <= S + 1) run
+// as slots (a; b1, b2): one N=256 MMA stream of A_a against B_b1 and B_b2
+// stacked.  Even levels L pair with L + 1: slots (a; L - a, L + 1 - a) for
+// a < L cover all of level L and all but (L, 1) of level L + 1.  The pairs
+// left over, (L, 1), join the top level's product of the same a when S + 1
+// is even; the rest run alone (N=128).  Per digit a this is
+// ceil((S + 1 - a) / 2) slots, the fewest possible with one A digit per
+// MMA: 9 slots for the 15 products of S=5, 16 for the 28 of S=7.  Slots with
+// the same pair of levels form a group (one accumulator, one shift per half).
+struct SlotDef {
+  unsigned char s, t1, t2;  // 0-based digits; t2 = NO_SLICE: single
+};
+struct SlotGroup {
+  unsigned char first, count, l1, l2;  // 0-based levels (s + t), l2 = NO_SLICE: single
+};
+struct SlotPlan {
+  std::vector<SlotDef> slots;
+  std::vector<SlotGroup> groups;
+};
+
+SlotPlan make_slot_plan(int S) {
+  std::vector<std::array<int, 3>> raw;  // 1-based (a, b1, b2), b2 = 0: single
+  std::vector<std::array<int, 2>> left, top;
+  for (int L = 2; L <= S + 1; L += 2) {
+    if (L + 1 <= S + 1) {
+      for (int a = 1; a < L; ++a) raw.push_back({a, L - a, L + 1 - a});
+      left.push_back({L, 1});  // (L, 1) of level L + 1
+    } else {
+      for (int a = 1; a <= S; ++a) top.push_back({a, S + 1 - a});
+    }
+  }
+  for (const auto& l : left) {
+    auto it = std::find_if(top.begin(), top.end(), [&](const std::array<int, 2>& t) {
+      return t[0] == l[0] && t[1] != l[1];
+    });
+    if (it != top.end()) {
+      raw.push_back({l[0], l[1], (*it)[1]});
+      top.erase(it);
+    } else {
+      raw.push_back({l[0], l[1], 0});
+    }
+  }
+  for (const auto& t : top) raw.push_back({t[0], t[1], 0});
+  // group by level pair, keeping the order of first appearance
+  std::vector<std::pair<int, int>> keys;
+  for (const auto& r : raw) {
+    const std::pair<int, int> k{r[0] + r[1] - 2, r[2] ? r[0] + r[2] - 2 : -1};
+    if (std::find(keys.begin(), keys.end(), k) == keys.end()) keys.push_back(k);
+  }
+  SlotPlan plan;
+  for (const auto& k : keys) {
+    SlotGroup g{(unsigned char)plan.slots.size(), 0, (unsigned char)k.first,
+                (unsigned char)(k.second < 0 ? NO_SLICE : k.second)};
+    for (const auto& r : raw)
+      if (r[0] + r[1] - 2 == k.first && (r[2] ? r[0] + r[2] - 2 : -1) == k.second) {
+        plan.slots.push_back({(unsigned char)(r[0] - 1), (unsigned char)(r[1] - 1),
+                              (unsigned char)(r[2] ? r[2] - 1 : NO_SLICE)});
+        g.count++;
+      }
+    plan.groups.push_back(g);
+  }
+  return plan;
+}
+
+const SlotPlan& slot_plan(int S) {
+  static const std::vector<SlotPlan> plans = [] {
+    std::vector<SlotPlan> v;
+    for (int s = 0; s <= MAX_SLICES; ++s) v.push_back(s ? make_slot_plan(s) : SlotPlan{});
+    return v;
+  }();
+  return plans[S];
+}
+
 }  // namespace
 
 int SplitEngine::reserve(int max_rows, int max_k, int batch_hint) {
@@ -721,6 +845,10 @@ int SplitEngine::reserve(int max_rows, int max_k, int batch_hint) {
   const int h = round_up(std::max(max_k / 2, 1), BM);
   const size_t batch = (size_t)std::max(batch_hint, 1) * item_bytes(MAX_SLICES, h, h, h);
   return ensure_ws(std::max(one, std::min(batch, (size_t)1 << 30)) + 1024);
+}
+
+int SplitEngine::slots(int S) {
+  return S >= 1 && S <= MAX_SLICES ? (int)slot_plan(S).slots.size() : 0;
 }
 
 bool SplitEngine::supports(const GemmDesc& g) const {
@@ -747,7 +875,6 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
                     g.triB == TRI_NONE;
   const size_t per_item = item_bytes(S, RpA, same ? 0 : RpB, Kp);
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>(g.batch, ws_bytes_ / per_item));
-  // the split itself: pairs (s, t) with s + t <= S + 1, ordered by level
   SplitParams p;
   std::memset(&p, 0, sizeof(p));
   p.m = g.m; p.n = g.n; p.k = g.k;
@@ -755,35 +882,24 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
   // bound of the fixed-point accumulator: K * 2^(beta*(S+1) - 2) * 1.03 must stay below 2^62
   const double lg = std::log2((double)g.k * 1.03) + beta * (S + 1) - 2;
   p.cs = std::max(0, (int)std::ceil(lg) - 62);
-  int np = 0;
-  for (int lvl = 2; lvl <= S + 1; ++lvl)
-    for (int a = 1; a < lvl; ++a) {
-      const int b = lvl - a;
-      if (a <= S && b <= S && np < MAXPAIRS) {
-        p.ps[np] = (unsigned char)(a - 1);
-        p.pt[np] = (unsigned char)(b - 1);
-        ++np;
-      }
-    }
-  p.npairs = np;
-  // groups: a level's pairs in groups of at most G, G * SBK terms per exact sum
-  {
-    const int G = std::max(1, EXACT_TERMS / SBK);
-    int ng = 0, off = 0;
-    for (int l = 0; l < S; ++l) {
-      const int cnt = l + 1, parts = (cnt + G - 1) / G;
-      for (int q = 0; q < parts && ng < MAXGROUPS; ++q) {
-        const int sz = cnt / parts + (q < cnt % parts ? 1 : 0);
-        p.g0[ng] = (unsigned char)off;
-        p.gs[ng] = (unsigned char)sz;
-        p.glevel[ng] = (unsigned char)l;
-        p.gchunk[ng] = (unsigned char)std::max(1, G / sz);
-        off += sz;
-        ++ng;
-      }
-    }
-    p.ngroups = ng;
+  const SlotPlan& plan = slot_plan(S);
+  p.nslots = (int)plan.slots.size();
+  for (int q = 0; q < p.nslots; ++q) {
+    p.ss[q] = plan.slots[q].s;
+    p.st1[q] = plan.slots[q].t1;
+    p.st2[q] = plan.slots[q].t2;
   }
+  p.ngroups = (int)plan.groups.size();
+  for (int gi = 0; gi < p.ngroups; ++gi) {
+    const SlotGroup& gr = plan.groups[gi];
+    p.g0[gi] = gr.first;
+    p.gs[gi] = gr.count;
+    p.gl1[gi] = gr.l1;
+    p.gl2[gi] = gr.l2;
+    // every half sums count * chunk * SBK products of at most 2^14: exact in FP32
+    p.gchunk[gi] = (unsigned char)std::max(1, EXACT_TERMS / (SBK * gr.count));
+  }
+  const int np = S * (S + 1) / 2;  // digit-pair products per output tile and K term
   p.triA = g.triA; p.triB = g.triB; p.outLower = g.outLower;
   p.ldc = g.ldc; p.ldd = g.ldd; p.sC = g.sC; p.sD = g.sD;
   p.alpha = g.alpha; p.betac = g.beta;

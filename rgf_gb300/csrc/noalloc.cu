@@ -6,12 +6,12 @@
 // for the whole device, or an embedding that hands in pre-placed device
 // buffers and forbids hidden allocations.  rgf_residual_norm_noalloc serves
 // them: the caller passes device inputs and a device output, and the only
-// scratch (the product A x, one double per row) lives in the fixed array
-// below, which the module holds on every GPU that loads this library until
-// the process exits.
+// scratch (the product A x, one double per row, plus an error flag) lives in
+// the fixed array below, which the module holds on every GPU that loads this
+// library until the process exits.  With lazy module loading (the CUDA
+// default) the module, and with it the array, is loaded on a device by the
+// first call there.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/rgf.h"
 #include "rgf_internal.h"
@@ -19,35 +19,26 @@
 namespace {
 
 constexpr size_t kNoAllocMaxN = RGF_NOALLOC_MAX_N;
-constexpr int kMaxDevices = 64;
+// doubles after the A x scratch: room for the bad-index flag (one int)
+constexpr size_t kFlagSlots = 32;
 
-// Scratch for A x; every call shares it and it keeps the last call's values.
-static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxN];
+// Scratch for A x, then the flag; every call shares it and it keeps the last
+// call's values (both parts are cleared at the start of each call).
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxN + kFlagSlots];
 
-std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device.  Host code may
+// Device address of the scratch array in the current context.  Host code may
 // not pass &g_noalloc_scratch to a kernel (that is a host-side stand-in), so
-// the address is looked up once per device, with that device current.
+// the address is looked up on every call, with the caller's device current;
+// the lookup allocates nothing and also follows a context that was reset and
+// created again.
 int scratch_for_current_device(double** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
     cudaGetLastError();
-    return RGF_ECUDA;
+    return e == cudaErrorMemoryAllocation ? RGF_ENOMEM : RGF_ECUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) return RGF_ENOTSUP;
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return RGF_ECUDA;
-    }
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<double*>(p);
   return RGF_OK;
 }
 
@@ -58,12 +49,17 @@ extern "C" int rgf_residual_norm_noalloc(size_t n, const size_t* d_ia, const siz
                                          const double* d_b, double* d_out, void* stream) {
   if (!d_ia || !d_ja || !d_a || !d_x || !d_b || !d_out) return RGF_EINVAL;
   if (n == 0 || n > kNoAllocMaxN) return RGF_EINVAL;
+  // An error the caller left pending is the caller's: report it without
+  // clearing it instead of launching on a context that may be broken.
+  if (cudaPeekAtLastError() != cudaSuccess) return RGF_ECUDA;
   double* scratch = nullptr;
   const int st = scratch_for_current_device(&scratch);
   if (st) return st;
-  // launch_residual zeroes the first n scratch entries before accumulating.
-  rgf::launch_residual((long long)n, d_ia, d_ja, d_a, d_x, d_b, scratch, d_out,
-                       static_cast<cudaStream_t>(stream));
-  const cudaError_t e = cudaGetLastError();
+  int* bad = reinterpret_cast<int*>(scratch + kNoAllocMaxN);
+  // zeroes scratch[0, n) and the flag, then accumulates A x and the norms;
+  // rows outside [c, n) in column c are skipped and make d_out NaN
+  const cudaError_t e = rgf::launch_residual((long long)n, d_ia, d_ja, d_a, d_x, d_b, scratch,
+                                             d_out, bad, static_cast<cudaStream_t>(stream));
+  if (e == cudaErrorMemoryAllocation) return RGF_ENOMEM;
   return e == cudaSuccess ? RGF_OK : RGF_ECUDA;
 }

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -94,6 +95,7 @@ struct rgf_handle {
   SplitEngine* split_side = nullptr;  // own slice workspace for the side stream
   // tuning knobs (rgf_set_tuning / rgf_autotune); knob_gen counts changes so
   // that a batch graph captured with older knobs is captured again
+  int leaf_wait_polls = 0;   // poll limit of the leaf's pivot waits (0 = default)
   int nb = 32;               // leaf width of the panel Cholesky (16, 32 or 64)
   double split_bias = 1.0;   // the estimated split-product time is scaled by it
   double tuned_ms = 0.0;     // factorize + RGFdiag time measured by the autotuner
@@ -115,6 +117,25 @@ struct rgf_handle {
   double timer_ms[3] = {0, 0, 0}, timer_flops[3] = {0, 0, 0}, timer_tflops = 0.0;
   long long timer_launches[3] = {0, 0, 0};
 };
+
+namespace rgf {
+// allocations left before the injected failure; < 0: injection off
+static std::atomic<long long> g_fail_alloc_after{-1};
+
+cudaError_t device_malloc(void** p, size_t bytes) {
+  long long left = g_fail_alloc_after.load();
+  while (left >= 0) {
+    if (g_fail_alloc_after.compare_exchange_weak(left, left - 1)) {
+      if (left == 0) {  // this allocation fails, later ones succeed again
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+      }
+      break;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+}  // namespace rgf
 
 namespace {
 
@@ -141,7 +162,7 @@ __global__ void status_init_kernel(DevStatus* st) {
 template <class T>
 int dalloc(rgf_handle* h, T** p, size_t count) {
   if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  cudaError_t e = device_malloc((void**)p, count * sizeof(T));
   if (e != cudaSuccess) {
     *p = nullptr;
     cudaGetLastError();
@@ -207,11 +228,12 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
     // Route by estimated time (fitted to per-shape timings on GB300).  A split
     // product costs ~50 us of pipeline start-up and drains, its slicing
     // (~10 us for K <= 512, ~25 us above, plus operand traffic), and per
-    // 148-tile wave ~100 ns per 128x128x16 slice MMA; the FP64 DMMA kernel
+    // 148-tile wave ~100 ns per K=16 step of each MMA stream (an N=256 or
+    // N=128 slice MMA; SplitEngine::slots streams per tile); the FP64 DMMA kernel
     // costs ~9 us of launches and runs at ~0.9 TFLOP/s.  Small or thin
     // products are faster in FP64 (which is also FP64-accurate).
     const int S = slices > 0 ? slices : eng->slices();
-    const double pairs = S * (S + 1) / 2.0;
+    const double streams = SplitEngine::slots(S);
     auto up = [](double x, double m) { return std::ceil(x / m) * m; };
     const double kq = up(g.k, 128);
     double tiles = up(g.m, 128) / 128.0 * (up(g.n, 128) / 128.0) * g.batch;
@@ -220,7 +242,7 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
     const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB;
     const double t_slice = (kq <= 512 ? 10e-6 : 25e-6) +
                            (g.m + (same ? 0.0 : g.n)) * kq * 8.0 * g.batch / 3e12;
-    const double t_split = 50e-6 + t_slice + waves * pairs * (kq / 16.0) * 100e-9;
+    const double t_split = 50e-6 + t_slice + waves * streams * (kq / 16.0) * 100e-9;
     const double t_fp64 = 9e-6 + gemm_flops(g) / 0.9e12;
     split = t_split * h->split_bias < t_fp64;
   }
@@ -240,7 +262,7 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
 }
 
 void leaf_potrf(rgf_handle* h, double* T, long long ldt, int nbk, int col0) {
-  launch_leaf_potrf(T, ldt, nbk, col0, h->d_status, cur_stream(h));
+  launch_leaf_potrf(T, ldt, nbk, col0, h->d_status, cur_stream(h), h->leaf_wait_polls);
   h->kernels_issued++;
 }
 
@@ -1135,8 +1157,8 @@ int rgf_residual_norm(rgf_handle* h, const double* x, const double* b, double* n
   if (!h->d_res && (st = dalloc(h, &h->d_res, 3 * n))) return st;
   RGF_CK(cudaMemcpyAsync(h->d_res, x, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   RGF_CK(cudaMemcpyAsync(h->d_res + n, b, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
-  launch_residual(n, h->d_ia, h->d_ja, h->d_a, h->d_res, h->d_res + n, h->d_res + 2 * n,
-                  h->d_scalars + 1, h->stream);
+  RGF_CK(launch_residual(n, h->d_ia, h->d_ja, h->d_a, h->d_res, h->d_res + n, h->d_res + 2 * n,
+                         h->d_scalars + 1, nullptr, h->stream));
   double out[2];
   RGF_CK(cudaMemcpyAsync(out, h->d_scalars + 1, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
   RGF_CK(cudaStreamSynchronize(h->stream));
@@ -1271,6 +1293,20 @@ int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m,
   delete eng;
   cudaFree(st);
   return status;
+}
+
+int rgf_debug_fail_alloc_after(long long after) {
+  rgf::g_fail_alloc_after.store(after < 0 ? -1 : after);
+  return RGF_OK;
+}
+
+int rgf_set_wait_limit(rgf_handle* h, int polls) {
+  if (!h || polls < 0) return RGF_EINVAL;
+  if (polls == h->leaf_wait_polls) return RGF_OK;
+  const int st = drop_graphs(h);  // the limit is a kernel argument of the captured stages
+  if (st) return st;
+  h->leaf_wait_polls = polls;
+  return RGF_OK;
 }
 
 int rgf_measure_fp64_peak(double* tflops) {

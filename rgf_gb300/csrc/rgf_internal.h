@@ -69,8 +69,16 @@ int launch_gemm_fp64(const GemmDesc& g, cudaStream_t s);
 
 // Cholesky of the nbk x nbk (nbk <= 64) lower tile at T (column-major, ldt),
 // in place.  Records the first non-positive pivot (global column col0 + j) in st.
+// Each wait of a column for the previous pivot polls at most wait_polls times
+// (0 = LEAF_WAIT_POLLS); a wait that runs out records a timeout in st and the
+// leaf stops updating.
+constexpr int LEAF_WAIT_POLLS = 1 << 26;
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* st,
-                       cudaStream_t s);
+                       cudaStream_t s, int wait_polls = 0);
+
+// Every device allocation of the library goes through here (so that a test
+// can make one fail: rgf_debug_fail_alloc_after).  cudaMalloc semantics.
+cudaError_t device_malloc(void** p, size_t bytes);
 
 // Row-parallel triangular solve with an nbk x nbk (nbk <= 64) lower tile L:
 //   mode 0: X := X * L^{-T}   (forward,  "R L T N")
@@ -110,10 +118,14 @@ void launch_set_identity(double* X, long long ld, int m, int batch, long long st
 void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,
                  int batch, long long sX, long long sY, cudaStream_t s);
 // r = b - A x (symmetric, from the lower CSC) for the first column; then
-// out[0] = ||r||_2, out[1] = ||b||_2.  scratch: n doubles.
-void launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
-                     const double* x, const double* b, double* scratch, double* out,
-                     cudaStream_t s);
+// out[0] = ||r||_2, out[1] = ||b||_2 (scaled sums of squares, as dnrm2).
+// scratch: n doubles.  CSC entries outside the lower triangle or past row n-1
+// are skipped; with `bad` (device int, may be null) they set *bad and both
+// outputs become NaN.  Returns the first launch error (the caller's pending
+// errors are the caller's to check first).
+cudaError_t launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
+                            const double* x, const double* b, double* scratch, double* out,
+                            int* bad, cudaStream_t s);
 // R = B - A X for nrhs columns (ld n) from the lower CSC; Y is n*nrhs scratch
 void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size_t* ja,
                              const double* a, const double* X, const double* B, double* Y,

@@ -24,6 +24,9 @@ class SplitEngine {
   // prepared sizes; batched problems run in chunks that fit the workspace).
   bool supports(const GemmDesc& g) const;
   int slices() const { return slices_; }
+  // MMA streams per output tile and K term at S slices (each one N=256 MMA
+  // of one A digit against two B digits, or N=128 against one)
+  static int slots(int S);
   int min_k() const { return min_k_; }
   // Issue D = alpha op(A) op(B) + beta C on stream s; returns kernels launched
   // and, in *tensor_flops (if given), the bf16 slice-product flops it runs.

@@ -12,7 +12,7 @@ x (solve), diag (the reference's RGFdiag), logdet, res, resn, plus a dense
 LAPACK diag(inv(A)) and logdet for the exact values.  Also stores the
 stdout of the reference's own main.C driver on A_11 (ref_main_A11.txt).
 
-Needs the reference tree (/root/reference or $RGF_REFERENCE) and g++; run
+Needs the reference tree (located by oracle/replay/build_replay.py) and g++; run
 it on a development machine: python tests/golden/make_golden.py
 """
 import os

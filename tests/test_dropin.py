@@ -11,7 +11,9 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_MAIN = os.path.join(os.environ.get("RGF_REFERENCE", "/root/reference"), "main.C")
+from oracle.replay.build_replay import reference_root  # noqa: E402
+
+REF_MAIN = os.path.join(reference_root(), "main.C")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_MAIN), reason="reference sources not present")

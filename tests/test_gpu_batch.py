@@ -33,3 +33,30 @@ def test_batch_matches_alone_and_oracle(rgf, precision, ltol, dtol):
         assert abs(ld[i] - ref["logdet"]) <= ltol * abs(ref["logdet"])
         assert np.max(np.abs(diags[i] - ref["diag"]) / np.abs(ref["diag"])) <= dtol
     assert b.kernels() > 0
+
+
+@pytest.mark.parametrize("precision,ltol,dtol", [("fp64", 1e-12, 1e-10), ("split", 1e-9, 1e-8)])
+def test_batch_workload_classes_vs_oracle(rgf, precision, ltol, dtol):
+    """One instance of every (ns, nd) class of the batched workload
+    (ns in {42, 128, 256, 512}, nd in {0, 2, 6}, nt drawn from [3, 60], seed 4)
+    in one batch graph: each equals the instance alone, bitwise, and matches
+    the oracle."""
+    rng = np.random.default_rng(4)
+    inst = []
+    for ns in (42, 128, 256, 512):
+        for nd in (0, 2, 6):
+            nt = int(rng.integers(3, 61))
+            ia, ja, a = gen.generate_bta(ns, nt, nd, 400 + len(inst))
+            inst.append((ia, ja, a, ns, nt, nd))
+    b = rgf.RGFBatch(inst, precision=precision)
+    b.run(concurrent=True)
+    ld, diags = b.run(concurrent=True)  # replay of the captured graph
+    for i, (ia, ja, a, ns, nt, nd) in enumerate(inst):
+        s = rgf.RGF(ia, ja, a, ns, nt, nd, precision=precision)
+        assert ld[i] == s.logDet()
+        assert np.array_equal(diags[i], s.RGFdiag())
+        s.close()
+        ref = O.run_all(ns, nt, nd, ia, ja, a, exact=True)
+        assert abs(ld[i] - ref["logdet"]) <= ltol * abs(ref["logdet"]), (ns, nt, nd)
+        assert np.max(np.abs(diags[i] - ref["diag"]) / np.abs(ref["diag"])) <= dtol, (ns, nt, nd)
+    b.close()

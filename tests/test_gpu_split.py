@@ -104,3 +104,25 @@ def test_split_solver_parity(rgf, ns, nt, nd, fp64_diag):
     assert np.max(np.abs(x - ref["x"])) <= 1e-12 * np.max(np.abs(ref["x"]))
     for q in range(2):
         assert O.residual_norm_normalized(ia, ja, a, x[:, q], b[:, q]) <= 1e-13
+
+
+def test_split_solver_ns1000_nt50_nd4_spde_vs_oracle(rgf):
+    """The ns=1000, nt=50, nd=4 workload (5-point SPDE operator on a 40 x 25
+    grid plus the dense random term, seed 2) in split precision against the
+    oracle's FP64 block recursion: logDet, RGFdiag and an 8-RHS refined solve."""
+    ns, nt, nd = 1000, 50, 4
+    ia, ja, a = gen.generate_bta(ns, nt, nd, 2, spde_grid=(40, 25))
+    n = ns * nt + nd
+    b = gen.random_rhs(n, 8, 2)
+    s = rgf.RGF(ia, ja, a, ns, nt, nd, precision="split")
+    ld = s.logDet()
+    d = s.RGFdiag()
+    x = s.solve(np.empty_like(b), b, 8)
+    ref = O.run_all(ns, nt, nd, ia, ja, a, b=b, exact=True)
+    assert abs(ld - ref["logdet"]) <= LOGDET_TOL * abs(ref["logdet"])
+    assert np.max(np.abs(d - ref["diag"]) / np.abs(ref["diag"])) <= DIAG_TOL
+    for q in range(8):
+        assert s.residualNormNormalized(np.ascontiguousarray(x[:, q]),
+                                        np.ascontiguousarray(b[:, q])) <= 1e-13
+    assert np.max(np.abs(x - ref["x"])) <= 1e-10 * np.max(np.abs(ref["x"]))
+    s.close()
