@@ -577,6 +577,19 @@ def run_rgf(args, w):
     ms_total = e0.elapsed_time(e1)
     launches = s.info()["kernels_launched"] - k0
     logdet = s.logDet()
+    # per-stage times of one more step (graph replays, events on the handle's
+    # stream): factorize + logDet, then the selected inversion (with the
+    # diagonal-block inverses it starts with)
+    q = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    q[0].record(stream)
+    s.factorize(); s.logDet()
+    q[1].record(stream)
+    s.diag_device_ptr()
+    q[2].record(stream)
+    q[2].synchronize()
+    stages = {"factorize_logdet_ms": q[0].elapsed_time(q[1]),
+              "selinv_ms": q[1].elapsed_time(q[2])}
     # per-class kernel times: one more (untimed) step with CUDA events around
     # every GEMM launch, each product run alone (serialised, warm)
     s.kernel_timer(2 if os.environ.get("RGF_GB300_TIMER_DETAIL") else 1)
@@ -749,7 +762,7 @@ def run_rgf(args, w):
                          "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "parts": e2e_parts} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
-                "plain_fp64": plain, "split_native_fp64_diag": native_diag,
+                "stages": stages, "plain_fp64": plain, "split_native_fp64_diag": native_diag,
                 "solve": solve_info, "oracle_err": oracle_err,
                 "clocks": clk, "logdet": logdet,
                 "timed_region": "each stage replayed as one CUDA graph; kernel classes timed "

@@ -184,12 +184,11 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
 // ---------------------------------------------------------------------------
 // Leaf Cholesky of one <= 64 x 64 diagonal tile in shared memory.
 // On GB300 each SM sub-partition has its own FP64 unit; one FP64 warp
-// instruction occupies it ~80 cycles and a dependent FP64 op waits ~64, so the
-// column-to-column pivot chain (next pivot update, its reciprocal square root)
-// is the critical path.  The tile keeps unscaled columns (updates use the
-// factor S[c][j] * y_j^2, y_j = S_jj^{-1/2}); all scaling to L happens in one
-// parallel pass at the end.  The log-determinant is summed later from the
-// factor's diagonal, off this path.
+// instruction occupies it ~76 cycles whatever the number of active lanes, and
+// a dependent FP64 op waits ~63 (measured), so the column-to-column pivot
+// chain (the next pivot's update, its reciprocal square root, the column's
+// scaling) is the critical path.  The log-determinant is summed later from
+// the factor's diagonal, off this path.
 // ---------------------------------------------------------------------------
 // float -> double by bit manipulation (no FP64 conversion instruction);
 // zero and subnormal floats give zero
@@ -237,16 +236,9 @@ __device__ __forceinline__ double rsqrt_fast(double d) {
 
 
 // ---------------------------------------------------------------------------
-// Leaf Cholesky, data-flow form.  Column c of the tile is owned by warp c % 8
-// (two warps per sub-partition, so all four FP64 units work).  Step j applies
-// column j (final, unscaled, with y_j = S_jj^{-1/2}) to every later column;
-// the owner of column j + 1 updates that column first, takes its pivot from
-// the register that holds the new diagonal and publishes y_{j+1} with a
-// release store, so step j + 1 starts in every warp as soon as its own step-j
-// columns are done and y_{j+1} is visible -- there is no CTA-wide barrier per
-// column.  Columns are written only by their owner; column j is read-only
-// once y_j is published.  Waits are bounded: after ~2^26 polls the kernel
-// records a timeout and every warp leaves the loop.
+// Leaf Cholesky, data-flow form: warps hand columns to each other through
+// release/acquire on a shared-memory counter (no CTA-wide barrier per
+// column); see leaf_chol below.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void st_release_cta(int* p, int v) {
   asm volatile("st.release.cta.shared::cta.b32 [%0], %1;"
@@ -259,103 +251,68 @@ __device__ __forceinline__ int ld_acquire_cta(const int* p) {
   return v;
 }
 
-__global__ void __launch_bounds__(256) leaf_potrf_flow_kernel(double* T, long long ldt, int nbk,
-                                                              int col0, DevStatus* st,
-                                                              int wait_polls) {
-  __shared__ double S[64][65];
-  __shared__ double ys[64];
-  __shared__ int ready;   // y_0 .. y_ready are published
-  __shared__ int abort_;  // a wait gave up
-  __shared__ int fail;    // smallest non-positive pivot column
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const double nan = __longlong_as_double(0x7ff8000000000000LL);
-  for (int c = warp; c < nbk; c += 8)
-    for (int r = c + lane; r < nbk; r += 32) S[r][c] = T[(long long)r + (long long)c * ldt];
-  if (tid == 0) {
-    fail = 0x7fffffff;
-    abort_ = 0;
-    ready = -1;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    const double d = S[0][0];
-    if (!(d > 0.0)) fail = 0;
-    ys[0] = d > 0.0 ? rsqrt_fast(d) : nan;
-    st_release_cta(&ready, 0);
-  }
-  for (int j = 0; j + 1 < nbk; ++j) {
-    if (ld_acquire_cta(&ready) < j) {
-      // bounded: after wait_polls polls the leaf gives up and records a timeout
-      int it = 0;
-      while (ld_acquire_cta(&ready) < j && !abort_ && ++it < wait_polls) {
-      }
-      if (it >= wait_polls) {
-        abort_ = 1;
-        if (lane == 0) atomicExch(&st->timeout, 1);
-      }
-      if (abort_) break;
-    }
-    const double y = ys[j];
-    const double y2 = y * y;
-    int c = j + 1 + ((warp - (j + 1)) % 8 + 8) % 8;  // first owned column > j
-    for (; c < nbk; c += 8) {
-      const double f = S[c][j] * y2;
-      double dnew = 0.0;
-      for (int r = c + lane; r < nbk; r += 32) {
-        const double v = fma(-S[r][j], f, S[r][c]);
-        S[r][c] = v;
-        if (r == c) dnew = v;
-      }
-      if (c == j + 1) {
-        __syncwarp();
-        if (lane == 0) {
-          const bool ok = dnew > 0.0;
-          if (!ok) atomicMin(&fail, c);
-          ys[c] = ok ? rsqrt_fast(dnew) : nan;
-          st_release_cta(&ready, c);
-        }
-      }
-    }
-  }
-  __syncthreads();
-  for (int c = warp; c < nbk; c += 8) {
-    const double y = ys[c];
-    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c] * y;
-  }
-  if (tid == 0 && fail != 0x7fffffff) atomicMin(&st->not_spd_col, col0 + fail);
+// The leaf Cholesky proper, on the tile held in shared memory S (lower part).
+// Column c belongs to warp c % 8.  Step j applies the final column j of L to
+// every later column (one FMA per column and 32 rows: L_cj is a broadcast
+// read); the owner of column j + 1 does that column first, then takes its
+// pivot d from shared memory in every lane (rsqrt on all lanes costs the same
+// warp instruction as on one), scales the column to its final value
+// (L_rc = S_rc d^{-1/2}, L_cc = d d^{-1/2}) and publishes it with a release
+// store.  FP64 ops on the pivot chain per column: FMA, the four of rsqrt_fast,
+// one multiply.  Columns are written only by their owner; column j is
+// read-only once published.  Waits are bounded by wait_polls polls, after
+// which the leaf records a timeout and stops.
+__device__ __forceinline__ void leaf_finalize(double (*S)[65], int nbk, int c, int lane,
+                                              int* ready, int* fail) {
+  __syncwarp();
+  const double d = S[c][c];
+  const bool ok = d > 0.0;
+  const double y = ok ? rsqrt_fast(d) : __longlong_as_double(0x7ff8000000000000LL);
+  for (int r = c + lane; r < nbk; r += 32) S[r][c] = (r == c ? d : S[r][c]) * y;
+  if (!ok && lane == 0) atomicMin(fail, c);
+  __syncwarp();
+  if (lane == 0) st_release_cta(ready, c);
 }
 
-// ---------------------------------------------------------------------------
-// Row-parallel triangular solve with a <= 64 x 64 lower tile, warp-synchronous.
+__device__ void leaf_chol(double (*S)[65], int nbk, DevStatus* st, int wait_polls, int* ready,
+                          int* abort_, int* fail) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) leaf_finalize(S, nbk, 0, lane, ready, fail);
+  for (int j = 0; j + 1 < nbk; ++j) {
+    if (ld_acquire_cta(ready) < j) {
+      int it = 0;
+      while (ld_acquire_cta(ready) < j && !*(volatile int*)abort_ && ++it < wait_polls) {
+      }
+      if (it >= wait_polls) {
+        *(volatile int*)abort_ = 1;
+        if (lane == 0) atomicExch(&st->timeout, 1);
+      }
+      if (*(volatile int*)abort_) break;
+    }
+    int c = j + 1 + ((warp - (j + 1)) % 8 + 8) % 8;  // first owned column > j
+    for (; c < nbk; c += 8) {
+      const double lcj = S[c][j];
+      for (int r = c + lane; r < nbk; r += 32) S[r][c] = fma(-S[r][j], lcj, S[r][c]);
+      if (c == j + 1) leaf_finalize(S, nbk, c, lane, ready, fail);
+    }
+  }
+}
+
+// Row-parallel solve X := X L^{-T} (MODE 0) or X := X L^{-1} (MODE 1) of the
+// rows [r0, r0 + nthreads/8) of X against the nbk x nbk lower tile in Ls.
 // Eight lanes share one row: lane q of the group keeps the unknowns
 // l = q, q + 8, ... in registers.  Step j: the owner of x_j scales it, one
 // shuffle hands it to the other seven lanes, and each applies it to its own
 // unknowns -- no CTA barrier per column, so the column-to-column chain is a
-// multiply, a shuffle and a fused multiply-add.  A warp holds four rows and a
-// CTA of 4 warps 16 rows, so the FP64 work spreads over many SMs (each SM
-// retires only ~3.5 FP64 flops per cycle).
+// multiply, a shuffle and a fused multiply-add.
 // MODE 0: x_j = (b_j - sum_{l<j} x_l L_jl) / L_jj   (X L^T = B)
 // MODE 1: x_j = (b_j - sum_{l>j} x_l L_lj) / L_jj   (X L = B)
-// ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs, long long xcs,
-                                                         int rows, const double* L, long long ldl,
-                                                         int nbk, long long sX, long long sL) {
-  __shared__ double Ls[64][65];
-  __shared__ double rinv[64];
-  X += (long long)blockIdx.y * sX;
-  L += (long long)blockIdx.y * sL;
-  for (int idx = threadIdx.x; idx < 64 * 64; idx += 128) {
-    const int c = idx >> 6, r = idx & 63;
-    double v = 0.0;
-    if (r < nbk && c < nbk && r >= c) v = L[(long long)r + (long long)c * ldl];
-    Ls[r][c] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < 64) rinv[threadIdx.x] = (threadIdx.x < nbk) ? 1.0 / Ls[threadIdx.x][threadIdx.x] : 0.0;
-  __syncthreads();
+__device__ __forceinline__ void trsm_rows_body(double* X, long long xrs, long long xcs, int rows,
+                                               double (*Ls)[65], const double* rinv, int nbk,
+                                               long long r0) {
   const int lane = threadIdx.x & 31, q = lane & 7, gbase = lane & ~7;
-  const long long r = (long long)blockIdx.x * 16 + (threadIdx.x >> 3);
+  const long long r = r0 + (threadIdx.x >> 3);
   const bool live = r < rows;
   double u[8];
 #pragma unroll
@@ -389,6 +346,54 @@ __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs
       if (l < nbk) X[r * xrs + (long long)l * xcs] = u[t];
     }
   }
+}
+
+// Leaf Cholesky of the nbk x nbk lower tile T in one CTA (leaf_chol).  The
+// rows below the leaf are solved by a separate trsm_rows launch: folding that
+// solve into this launch (CTAs that wait for the leaf) was measured slower at
+// ns=2000, as the waiting CTAs hold SMs that the concurrent side-stream
+// products need.
+__global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ldt, int nbk,
+                                                         int col0, DevStatus* st, int wait_polls) {
+  __shared__ double S[64][65];
+  __shared__ int ready, abort_, fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int c = warp; c < nbk; c += 8)
+    for (int r = c + lane; r < nbk; r += 32) S[r][c] = T[(long long)r + (long long)c * ldt];
+  if (tid == 0) {
+    fail = 0x7fffffff;
+    abort_ = 0;
+    ready = -1;
+  }
+  __syncthreads();
+  leaf_chol(S, nbk, st, wait_polls, &ready, &abort_, &fail);
+  __syncthreads();
+  for (int c = warp; c < nbk; c += 8)
+    for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c];
+  if (tid == 0 && fail != 0x7fffffff) atomicMin(&st->not_spd_col, col0 + fail);
+}
+
+// Row-parallel triangular solve with a <= 64 x 64 lower tile (trsm_rows_body):
+// a warp holds four rows and a CTA of 4 warps 16 rows, so the FP64 work
+// spreads over many SMs (each SM retires only ~3.5 FP64 flops per cycle).
+template <int MODE>
+__global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs, long long xcs,
+                                                         int rows, const double* L, long long ldl,
+                                                         int nbk, long long sX, long long sL) {
+  __shared__ double Ls[64][65];
+  __shared__ double rinv[64];
+  X += (long long)blockIdx.y * sX;
+  L += (long long)blockIdx.y * sL;
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 128) {
+    const int c = idx >> 6, r = idx & 63;
+    double v = 0.0;
+    if (r < nbk && c < nbk && r >= c) v = L[(long long)r + (long long)c * ldl];
+    Ls[r][c] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 64) rinv[threadIdx.x] = (threadIdx.x < nbk) ? 1.0 / Ls[threadIdx.x][threadIdx.x] : 0.0;
+  __syncthreads();
+  trsm_rows_body<MODE>(X, xrs, xcs, rows, Ls, rinv, nbk, (long long)blockIdx.x * 16);
 }
 
 // Thin products (m <= 16, op(B) = B^T): lane = output column, the 4 warps of
@@ -599,8 +604,8 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* st,
                        cudaStream_t s, int wait_polls) {
   if (nbk <= 0) return;
-  leaf_potrf_flow_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, st,
-                                           wait_polls > 0 ? wait_polls : LEAF_WAIT_POLLS);
+  leaf_potrf_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, st,
+                                      wait_polls > 0 ? wait_polls : LEAF_WAIT_POLLS);
 }
 
 void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,
