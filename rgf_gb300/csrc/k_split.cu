@@ -88,6 +88,15 @@ struct SplitParams {
   int mD1;
   double alpha, betac;
   DevStatus* st;
+  // Split K over ksplit CTAs per output tile (blockIdx.z = batch item *
+  // ksplit + slice): slice kz runs the jobs j with j % ksplit == kz, adds its
+  // fixed-point partial sums to the tile's int64 workspace with atomics
+  // (integer sums: the result is the same bits whatever the order) and the
+  // CTA that arrives last at the tile's counter converts, writes D and sets
+  // workspace and counter back to zero.
+  int ksplit;
+  long long* wsk;  // 128 x 128 int64 per tile (column-major by tile column)
+  int* cnt;        // arrival counter per tile
 };
 
 // ---- PTX wrappers -----------------------------------------------------------
@@ -262,19 +271,24 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   uint64_t* mma_done = acc_empty + 2;                      // every MMA of this CTA retired
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* last_flag = reinterpret_cast<volatile int*>(tmem_slot + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   if (p.outLower && m0 + BM <= n0) return;  // whole tile above the diagonal (uniform exit)
-  const int zb = blockIdx.z;                // batch item: slice planes zb*S .. zb*S+S-1
+  const int zb = blockIdx.z / p.ksplit;     // batch item: slice planes zb*S .. zb*S+S-1
+  const int kz = blockIdx.z - zb * p.ksplit;
   const int zS = zb * p.S;
 
   int kb_lo, kb_hi;
   tile_kblocks(p, m0, n0, kb_lo, kb_hi);
   const int nkb = kb_hi - kb_lo;
-  // jobs: for each group, K chunks of gchunk stages
-  int njobs = 0;
-  for (int g = 0; g < p.ngroups; ++g) njobs += nkb > 0 ? (nkb + p.gchunk[g] - 1) / p.gchunk[g] : 0;
+  // jobs: for each group, K chunks of gchunk stages; this CTA runs every
+  // ksplit-th of them (all of them without split K)
+  int njobs_all = 0;
+  for (int g = 0; g < p.ngroups; ++g)
+    njobs_all += nkb > 0 ? (nkb + p.gchunk[g] - 1) / p.gchunk[g] : 0;
+  const int njobs = njobs_all > kz ? (njobs_all - kz + p.ksplit - 1) / p.ksplit : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
@@ -305,9 +319,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     if (lane == 0) {
       long long use = 0;
       bool ok = true;
+      int ja = 0;  // job index over all jobs of the tile
       for (int g = 0; g < p.ngroups && ok; ++g) {
         const int chunk = p.gchunk[g], q0 = p.g0[g], q1 = q0 + p.gs[g];
-        for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk) {
+        for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk, ++ja) {
+          if (ja % p.ksplit != kz) continue;
           const int kb1 = min(kb_hi, kb0 + chunk);
           for (int q = q0; q < q1 && ok; ++q) {
             const bool two = p.st2[q] != NO_SLICE;
@@ -338,11 +354,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       long long use = 0;
-      int j = 0;
+      int j = 0;   // job index among this CTA's jobs
+      int ja = 0;  // job index over all jobs of the tile
       bool ok = true;
       for (int g = 0; g < p.ngroups && ok; ++g) {
         const int chunk = p.gchunk[g], q0 = p.g0[g], q1 = q0 + p.gs[g];
-        for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk, ++j) {
+        for (int kb0 = kb_lo; kb0 < kb_hi && ok; kb0 += chunk, ++ja) {
+          if (ja % p.ksplit != kz) continue;
           const int kb1 = min(kb_hi, kb0 + chunk);
           const int buf = j & 1;
           const uint32_t aph = (uint32_t)((j >> 1) & 1);
@@ -370,6 +388,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
           if (!ok) break;
           umma_commit(&acc_full[buf]);  // accumulator ready for the drain warps
+          ++j;
         }
       }
       // One more commit tracks every MMA this thread issued: wait for it (also
@@ -385,13 +404,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     long long acc[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) acc[i] = 0;
-    int g = 0, jg = 0;  // group of job j and job index within the group
-    int nch = nkb > 0 && p.ngroups > 0 ? (nkb + p.gchunk[0] - 1) / p.gchunk[0] : 0;
-    for (int j = 0; j < njobs; ++j, ++jg) {
-      while (jg >= nch) {
-        ++g;
-        jg = 0;
-        nch = (nkb + p.gchunk[g] - 1) / p.gchunk[g];
+    int g = 0, gend = 0;  // group of job j; gend: first job index (over all jobs) after it
+    for (int j = 0; j < njobs; ++j) {
+      const int ja = kz + j * p.ksplit;  // index of this CTA's j-th job over all jobs
+      while (ja >= gend) {
+        if (gend > 0) ++g;
+        gend += (nkb + p.gchunk[g] - 1) / p.gchunk[g];
       }
       const int buf = j & 1;
       if (!mbar_wait(&acc_full[buf], (uint32_t)((j >> 1) & 1), abort_flag, p.st)) break;
@@ -420,9 +438,35 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
+    if (p.ksplit > 1) {
+      // split K: add this slice's partial sums to the tile's workspace; the
+      // last slice to arrive takes the total (and leaves zeros behind)
+      const long long tile =
+          blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * zb);
+      unsigned long long* W = reinterpret_cast<unsigned long long*>(p.wsk) + tile * (BM * BN);
+      if (!*abort_flag) {
+#pragma unroll
+        for (int i = 0; i < 64; ++i)
+          if (acc[i] != 0) atomicAdd(&W[(half * 64 + i) * BM + row], (unsigned long long)acc[i]);
+      }
+      __threadfence();
+      asm volatile("bar.sync 1, 256;" ::: "memory");  // the eight drain warps
+      if (warp == 2 && lane == 0) *last_flag = atomicAdd(&p.cnt[tile], 1) == p.ksplit - 1;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (*last_flag) {
+        __threadfence();
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+          unsigned long long* w = &W[(half * 64 + i) * BM + row];
+          acc[i] = (long long)__ldcg(w);
+          __stcg(w, 0ull);
+        }
+        if (warp == 2 && lane == 0) p.cnt[tile] = 0;
+      }
+    }
     // epilogue: one FP64 conversion per output
     const int r = m0 + row;
-    if (r < p.m && !*abort_flag) {
+    if (r < p.m && !*abort_flag && (p.ksplit == 1 || *last_flag)) {
       const int* exB = p.exB + (long long)zb * p.exB_stride;
       const bool hi = p.D2 && r >= p.mD1;
       const double* C = hi ? p.C2 + (long long)zb * p.sC - p.mD1
@@ -735,6 +779,36 @@ SplitEngine* SplitEngine::create(int slices, int* status) {
 
 SplitEngine::~SplitEngine() {
   if (ws_) cudaFree(ws_);
+  if (wsk_) cudaFree(wsk_);
+}
+
+int SplitEngine::ensure_splitk(long long tiles) {
+  if (tiles <= wsk_tiles_) return RGF_OK;
+  if (wsk_) cudaFree(wsk_);
+  wsk_ = nullptr;
+  cnt_ = nullptr;
+  wsk_tiles_ = 0;
+  const size_t bytes = (size_t)tiles * BM * BN * sizeof(long long) + (size_t)tiles * sizeof(int);
+  void* p = nullptr;
+  if (device_malloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return RGF_ENOMEM;
+  }
+  if (cudaMemset(p, 0, bytes) != cudaSuccess) {
+    cudaFree(p);
+    return RGF_ECUDA;
+  }
+  wsk_ = static_cast<long long*>(p);
+  cnt_ = reinterpret_cast<int*>(wsk_ + (size_t)tiles * BM * BN);
+  wsk_tiles_ = tiles;
+  return RGF_OK;
+}
+
+int SplitEngine::reset_splitk(cudaStream_t s) {
+  if (!wsk_) return RGF_OK;
+  const size_t bytes = (size_t)wsk_tiles_ * BM * BN * sizeof(long long) +
+                       (size_t)wsk_tiles_ * sizeof(int);
+  return cudaMemsetAsync(wsk_, 0, bytes, s) == cudaSuccess ? RGF_OK : RGF_ECUDA;
 }
 
 int SplitEngine::ensure_ws(size_t bytes) {
@@ -847,6 +921,37 @@ int SplitEngine::reserve(int max_rows, int max_k, int batch_hint) {
   return ensure_ws(std::max(one, std::min(batch, (size_t)1 << 30)) + 1024);
 }
 
+// Estimated device time of gemm(g) (seconds), fitted to GB300 timings of
+// this kernel: about 20 us of launches, pipeline fill and epilogue, the
+// slicing (about 8 us per launch plus the operands' FP64 reads and bf16
+// writes at ~3 TB/s), and per wave of CTAs 120 ns per K=16 step of each MMA
+// stream, divided over the split-K slices.
+double SplitEngine::estimate_seconds(const GemmDesc& g, int slices) const {
+  const int S = slices > 0 ? std::min(slices, MAX_SLICES) : slices_;
+  const int Kp = round_up(g.k, BKE);
+  const int tx = round_up(g.m, BM) / BM, ty = round_up(g.n, BN) / BN;
+  long long tiles = 0;
+  for (int bx = 0; bx < tx; ++bx)
+    for (int by = 0; by < ty; ++by)
+      if (!(g.outLower && bx * BM + BM <= by * BN)) ++tiles;
+  tiles *= g.batch;
+  const SlotPlan& plan = slot_plan(S);
+  int jobs = 0;
+  for (const SlotGroup& gr : plan.groups) {
+    const int chunk = std::max(1, EXACT_TERMS / (SBK * gr.count));
+    jobs += (Kp / SBK + chunk - 1) / chunk;
+  }
+  long long ksplit = 1;
+  if (wsk_ && tiles * 2 <= num_sms_ && (long long)tx * ty * g.batch <= wsk_tiles_)
+    ksplit = std::max<long long>(1, std::min<long long>({16, jobs, num_sms_ / std::max(1ll, tiles)}));
+  const double waves = std::ceil((double)(tiles * ksplit) / num_sms_);
+  const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB;
+  const double t_slice = (Kp <= SHORT_K ? 8e-6 : 16e-6) +
+                         (g.m + (same ? 0.0 : g.n)) * (double)Kp * (8.0 + 2.0 * S) * g.batch / 3e12;
+  const double steps = (double)plan.slots.size() * (Kp / 16.0) / ksplit;
+  return 20e-6 + t_slice + waves * steps * 120e-9;
+}
+
 int SplitEngine::slots(int S) {
   return S >= 1 && S <= MAX_SLICES ? (int)slot_plan(S).slots.size() : 0;
 }
@@ -860,7 +965,16 @@ bool SplitEngine::supports(const GemmDesc& g) const {
 int SplitEngine::prepare(int max_rows, int max_k, int batch_hint) {
   max_rows_ = round_up(std::max(max_rows, 1), BM);
   max_k_ = round_up(std::max(max_k, 1), BKE);
-  return reserve(max_rows_, max_k_, batch_hint);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return RGF_ECUDA;
+  }
+  int st = reserve(max_rows_, max_k_, batch_hint);
+  if (st) return st;
+  // split K serves launches whose tiles cover at most half of the SMs
+  return ensure_splitk(std::max(1, num_sms_ / 2));
 }
 
 long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
@@ -978,7 +1092,23 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
     p.C2 = g.C2 ? g.C2 + (long long)b0 * g.sC : nullptr;
     p.D2 = g.D2 ? g.D2 + (long long)b0 * g.sD : nullptr;
     p.mD1 = g.mD1;
-    dim3 grid(RpA / BM, RpB / BN, nbat);
+    // split K when the output tiles fill at most half of the SMs (and the
+    // workspace holds them): up to 16 slices of a tile's jobs, so that the
+    // launch covers about one wave
+    int ntiles = 0;
+    for (int bx = 0; bx < RpA / BM; ++bx)
+      for (int by = 0; by < RpB / BN; ++by)
+        if (!(g.outLower && bx * BM + BM <= by * BN)) ++ntiles;
+    const long long grid_tiles = (long long)(RpA / BM) * (RpB / BN) * nbat;
+    p.ksplit = 1;
+    if (wsk_ && (long long)ntiles * nbat * 2 <= num_sms_ && grid_tiles <= wsk_tiles_) {
+      int jobs = 0;  // jobs of a tile with the full K range
+      for (int gi = 0; gi < p.ngroups; ++gi) jobs += (Kp / SBK + p.gchunk[gi] - 1) / p.gchunk[gi];
+      p.ksplit = std::max(1, std::min({16, jobs, num_sms_ / (ntiles * nbat)}));
+    }
+    p.wsk = wsk_;
+    p.cnt = cnt_;
+    dim3 grid(RpA / BM, RpB / BN, nbat * p.ksplit);
     if (tensor_flops) {
       double tiles = 0.0;  // lower-only outputs skip tiles above the diagonal
       for (int bx = 0; bx < (int)grid.x; ++bx)

@@ -113,6 +113,17 @@ struct rgf_handle {
   bool timer_on = false;
   bool timer_detail_on = false;  // per-shape totals printed to stderr on timer reset
   std::vector<TimedLaunch> ev_used;
+  // launch trace (RGF_GB300_TRACE=<csv path>): stages run launch by launch and
+  // an event follows every launch on its stream
+  struct TraceRec {
+    std::string label;
+    int side;
+    cudaEvent_t ev;
+  };
+  std::string trace_path;
+  std::vector<TraceRec> trace;
+  cudaEvent_t trace_t0 = nullptr;
+  int trace_stage = 0;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
   double timer_ms[3] = {0, 0, 0}, timer_flops[3] = {0, 0, 0}, timer_tflops = 0.0;
   long long timer_launches[3] = {0, 0, 0};
@@ -196,6 +207,32 @@ void join_side(rgf_handle* h) {
   cudaStreamWaitEvent(h->stream, h->ev_join, 0);
 }
 
+// Launch trace: an event on the current stream after the launch just issued.
+void trace(rgf_handle* h, const char* label) {
+  if (h->trace_path.empty()) return;
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, cur_stream(h));
+  h->trace.push_back({label, h->on_side ? 1 : 0, e});
+}
+
+// Append the stage's trace to the CSV file: stage, launch, stream (0 main,
+// 1 side), label, ms from the stage start to the end of the launch.
+void trace_flush(rgf_handle* h) {
+  if (h->trace.empty()) return;
+  FILE* f = std::fopen(h->trace_path.c_str(), "a");
+  int i = 0;
+  for (auto& t : h->trace) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->trace_t0, t.ev);
+    if (f) std::fprintf(f, "%d,%d,%d,%s,%.4f\n", h->trace_stage, i++, t.side, t.label.c_str(), ms);
+    cudaEventDestroy(t.ev);
+  }
+  if (f) std::fclose(f);
+  h->trace.clear();
+  h->trace_stage++;
+}
+
 void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   if (g.m <= 0 || g.n <= 0 || g.batch <= 0) return;
   const bool bulk = cls != SMALL;
@@ -225,24 +262,11 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
   SplitEngine* eng = h->on_side ? h->split_side : h->split;
   bool split = eng && may_split && eng->supports(g);
   if (split) {
-    // Route by estimated time (fitted to per-shape timings on GB300).  A split
-    // product costs ~50 us of pipeline start-up and drains, its slicing
-    // (~10 us for K <= 512, ~25 us above, plus operand traffic), and per
-    // 148-tile wave ~100 ns per K=16 step of each MMA stream (an N=256 or
-    // N=128 slice MMA; SplitEngine::slots streams per tile); the FP64 DMMA kernel
-    // costs ~9 us of launches and runs at ~0.9 TFLOP/s.  Small or thin
-    // products are faster in FP64 (which is also FP64-accurate).
-    const int S = slices > 0 ? slices : eng->slices();
-    const double streams = SplitEngine::slots(S);
-    auto up = [](double x, double m) { return std::ceil(x / m) * m; };
-    const double kq = up(g.k, 128);
-    double tiles = up(g.m, 128) / 128.0 * (up(g.n, 128) / 128.0) * g.batch;
-    if (g.outLower && g.m == g.n) tiles = tiles * 0.5 + up(g.m, 128) / 256.0 * g.batch;
-    const double waves = std::ceil(tiles / 148.0);
-    const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB;
-    const double t_slice = (kq <= 512 ? 10e-6 : 25e-6) +
-                           (g.m + (same ? 0.0 : g.n)) * kq * 8.0 * g.batch / 3e12;
-    const double t_split = 50e-6 + t_slice + waves * streams * (kq / 16.0) * 100e-9;
+    // Route by estimated time: the split engine's estimate (its launches,
+    // slicing, MMA streams and split K) against the FP64 DMMA kernel at
+    // ~9 us of launches and ~0.9 TFLOP/s.  Small or thin products are faster
+    // in FP64 (which is also FP64-accurate).
+    const double t_split = eng->estimate_seconds(g, slices);
     const double t_fp64 = 9e-6 + gemm_flops(g) / 0.9e12;
     split = t_split * h->split_bias < t_fp64;
   }
@@ -255,6 +279,12 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
     launched = launch_gemm_fp64(gw, cur_stream(h));
   }
   h->kernels_issued += launched;
+  if (!h->trace_path.empty()) {
+    char lab[96];
+    std::snprintf(lab, sizeof(lab), "%s cls%d m%d n%d k%d b%d", split ? "split" : "fp64", cls, g.m,
+                  g.n, g.k, g.batch);
+    trace(h, lab);
+  }
   if (e0) {
     cudaEventRecord(e1, cur_stream(h));
     h->ev_used.push_back({e0, e1, split ? 2 : 1, gemm_flops(g), tflops, g.m, g.n, g.k, g.batch, cls});
@@ -264,6 +294,7 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
 void leaf_potrf(rgf_handle* h, double* T, long long ldt, int nbk, int col0) {
   launch_leaf_potrf(T, ldt, nbk, col0, h->d_status, cur_stream(h), h->leaf_wait_polls);
   h->kernels_issued++;
+  trace(h, "leaf");
 }
 
 void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
@@ -272,6 +303,11 @@ void trsm_rows(rgf_handle* h, double* X, long long xrs, long long xcs, int rows,
   if (rows <= 0) return;
   launch_trsm_rows(X, xrs, xcs, rows, L, ldl, nbk, mode, batch, sX, sL, cur_stream(h));
   h->kernels_issued++;
+  if (!h->trace_path.empty()) {
+    char lab[64];
+    std::snprintf(lab, sizeof(lab), "trsm rows%d nb%d b%d", rows, nbk, batch);
+    trace(h, lab);
+  }
 }
 
 // ---- panel Cholesky: [D; B; C] (rows x cols, lda) -> [L; B L^-T; C L^-T] ----
@@ -328,9 +364,10 @@ void panel_potrf(rgf_handle* h, double* P, long long lda, int rows, int cols, in
     upd(c1, cols - c1, DIAG);              // inside the diagonal block: FP64 accuracy
     upd(cols, split_row - cols, BULK);
   } else if (h->split && h->opts.fp64_diag) {
-    // a narrow node: both parts are FP64 products anyway, so one launch
-    // covers the diagonal block and the rows below it on the critical path
-    upd(c1, split_row - c1, SMALL);
+    // a narrow node: one launch covers the diagonal block and the rows below
+    // it on the critical path, at FP64 accuracy (7-slice split products or
+    // FP64, whichever the cost model finds faster)
+    upd(c1, split_row - c1, DIAG);
   } else {
     upd(c1, split_row - c1, BULK);
   }
@@ -346,6 +383,7 @@ void issue_factor(rgf_handle* h) {
   cudaMemsetAsync(h->d_MF, 0, sizeof(double) * h->mf_size, s);
   launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, s);
   h->kernels_issued += 2;
+  trace(h, "ingest");
   double* corner = h->d_MF + mf_col_offset(sh, nt);
   for (long long i = 0; i < nt; ++i) {
     double* P = h->d_MF + mf_col_offset(sh, i);
@@ -378,6 +416,7 @@ void issue_factor(rgf_handle* h) {
     }
     panel_potrf(h, P, lda, (int)lda, (int)ns, (int)ns, (int)(i * ns));
     if (h->lookahead && h->side && lda > ns) join_side(h);
+    trace(h, "block end");
   }
   if (nd > 0) {
     const double* Pl = h->d_MF + mf_col_offset(sh, nt - 1);
@@ -665,8 +704,12 @@ void issue_solve(rgf_handle* h, int nrhs) {
 // the stage runs launch by launch.
 template <class F>
 int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, int* runs, F issue) {
-  if (h->timer_on || !h->opts.use_graphs || (!*exec && (*runs)++ == 0)) {
+  if (h->timer_on || !h->trace_path.empty() || !h->opts.use_graphs || (!*exec && (*runs)++ == 0)) {
     h->kernels_issued = 0;
+    if (!h->trace_path.empty()) {
+      if (!h->trace_t0) cudaEventCreate(&h->trace_t0);
+      cudaEventRecord(h->trace_t0, h->stream);
+    }
     issue();
     h->kernels_total += h->kernels_issued;
     RGF_CK(cudaGetLastError());
@@ -720,9 +763,16 @@ int sync_and_check(rgf_handle* h) {
   RGF_CK(cudaStreamSynchronize(h->stream));
   RGF_CK(cudaGetLastError());
   if (h->timer_on) collect_timer(h);
+  trace_flush(h);
   DevStatus st;
   RGF_CK(cudaMemcpy(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost));
-  if (st.timeout) return RGF_ETIMEOUT;
+  if (st.timeout) {
+    // a split product that gave up may have left its split-K workspace dirty
+    for (SplitEngine* e : {h->split, h->split_side})
+      if (e) e->reset_splitk(h->stream);
+    cudaStreamSynchronize(h->stream);
+    return RGF_ETIMEOUT;
+  }
   if (st.bad_input) return RGF_EINVAL;
   if (st.not_spd_col != INT_MAX) {
     h->not_spd_col = st.not_spd_col;
@@ -803,6 +853,8 @@ void release(rgf_handle* h) {
   for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);
   for (auto& e : h->ev_used) { cudaEventDestroy(e.e0); cudaEventDestroy(e.e1); }
   for (auto& e : h->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& t : h->trace) cudaEventDestroy(t.ev);
+  if (h->trace_t0) cudaEventDestroy(h->trace_t0);
   delete h->split;
   delete h->split_side;
   void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
@@ -916,6 +968,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
       break;
     }
     if (const char* e = std::getenv("RGF_GB300_LOOKAHEAD")) h->lookahead = std::atoi(e) != 0;
+    if (const char* e = std::getenv("RGF_GB300_TRACE")) h->trace_path = e;
     if ((st = dalloc(h, &h->d_ia, n + 1))) break;
     if ((st = dalloc(h, &h->d_ja, h->nnz))) break;
     if ((st = dalloc(h, &h->d_a, h->nnz))) break;

@@ -27,22 +27,34 @@ class SplitEngine {
   // MMA streams per output tile and K term at S slices (each one N=256 MMA
   // of one A digit against two B digits, or N=128 against one)
   static int slots(int S);
+  // Estimated device time of gemm(g, ..., slices), in seconds.
+  double estimate_seconds(const GemmDesc& g, int slices = 0) const;
   int min_k() const { return min_k_; }
   // Issue D = alpha op(A) op(B) + beta C on stream s; returns kernels launched
   // and, in *tensor_flops (if given), the bf16 slice-product flops it runs.
   // slices > 0 overrides the engine's slice count (up to 8) for this call.
   long long gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
                  double* tensor_flops = nullptr, int slices = 0);
+  // Zero the split-K workspace and counters (they clear themselves after
+  // every launch that completes; a launch that gave up on a wait may leave
+  // them dirty).
+  int reset_splitk(cudaStream_t s);
 
  private:
   SplitEngine() = default;
   int ensure_ws(size_t bytes);
+  int ensure_splitk(long long tiles);
   int reserve(int max_rows, int max_k, int batch_hint);
   int slices_ = 0;
   int min_k_ = 1 << 30;
   int max_rows_ = 0, max_k_ = 0;
   void* ws_ = nullptr;
   size_t ws_bytes_ = 0;
+  int num_sms_ = 148;
+  // split K: int64 partial sums (128 x 128 per tile) and arrival counters
+  long long* wsk_ = nullptr;
+  int* cnt_ = nullptr;
+  long long wsk_tiles_ = 0;
 };
 
 }  // namespace rgf
