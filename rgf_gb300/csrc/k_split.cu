@@ -229,9 +229,46 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ double pow2(int e) {
-  if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
-  return ldexp(1.0, e);
+// v * 2^e as the nearest double (ties to even) with integer instructions
+// only -- on GB300 each FP64 warp instruction (conversions included) holds an
+// SM sub-partition's FP64 unit ~76 cycles, which a 128 x 128 tile's epilogue
+// would spend four times per output.  Same bits as rounding the exact value
+// once, subnormal results included.
+__device__ __forceinline__ double i64_ldexp(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll((long long)a);
+  int msb = 63 - lz;                               // a in [2^msb, 2^(msb + 1))
+  const unsigned long long m = a << lz;            // leading one at bit 63
+  unsigned long long mant = m >> 11;               // 53 significant bits
+  const unsigned long long rem = m & 0x7FFull;     // the 11 bits rounded away
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) {
+    ++mant;
+    if (mant >> 53) {
+      mant >>= 1;
+      ++msb;
+    }
+  }
+  const int E = msb + e + 1023;                    // biased exponent of the leading bit
+  if (E >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+  if (E <= 0) {  // below the normal range: a 2^e in units of 2^-1074, rounded
+    const int t = e + 1074;
+    unsigned long long q;
+    if (t >= 0) {
+      q = a << t;  // exact: the value is below 2^-1022
+    } else if (t > -64) {
+      const int r = -t;
+      q = a >> r;
+      const unsigned long long low = a & ((1ull << r) - 1), halfway = 1ull << (r - 1);
+      if (low > halfway || (low == halfway && (q & 1ull))) ++q;
+    } else {
+      q = 0;
+    }
+    return __longlong_as_double((long long)(sign | q));
+  }
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 // exact FP32 integer partial v, weighted by 2^sh into the fixed-point sum
@@ -464,22 +501,56 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         if (warp == 2 && lane == 0) p.cnt[tile] = 0;
       }
     }
-    // epilogue: one FP64 conversion per output
+    // epilogue: every output once, v = alpha acc 2^(er + exB[c]) + beta C.
+    // The accumulators go to the (now idle) pipeline shared memory and a
+    // compact loop converts eight columns per pass -- the C reads of the
+    // eight issued before any is used -- instead of a 64-fold unrolled body
+    // (large code, slow to issue).  The columns' exponents come from two
+    // coalesced loads per warp, shuffled to the lanes.  The conversion is
+    // integer arithmetic (i64_ldexp): the only FP64 instruction per output is
+    // the FMA with beta C.
     const int r = m0 + row;
-    if (r < p.m && !*abort_flag && (p.ksplit == 1 || *last_flag)) {
-      const int* exB = p.exB + (long long)zb * p.exB_stride;
-      const bool hi = p.D2 && r >= p.mD1;
-      const double* C = hi ? p.C2 + (long long)zb * p.sC - p.mD1
-                           : (p.C ? p.C + (long long)zb * p.sC : nullptr);
-      double* D = hi ? p.D2 + (long long)zb * p.sD - p.mD1 : p.D + (long long)zb * p.sD;
-      const int er = p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1) + 2;
-      const int cbase = n0 + half * 64;
+    const bool live = r < p.m && !*abort_flag && (p.ksplit == 1 || *last_flag);
+    const int t = threadIdx.x - 64;  // drain thread 0..255
+    long long* eacc = reinterpret_cast<long long*>(smem);  // 64 x 256 int64 = 128 KiB
+    // alpha and beta tests as integers, once (an FP64 compare per output
+    // would cost as much as the FMA); alpha = -1 is a negation of the integers
+    const int amode = p.alpha == 1.0 ? 0 : (p.alpha == -1.0 ? 1 : 2);
+    if (!*abort_flag) {
 #pragma unroll
-      for (int i = 0; i < 64; ++i) {
-        const int c = cbase + i;
-        if (c < p.n && !(p.outLower && r < c)) {
-          double v = p.alpha * ((double)acc[i] * pow2(er + exB[c]));
-          if (p.betac != 0.0) v += p.betac * C[(long long)r + (long long)c * p.ldc];
+      for (int i = 0; i < 64; ++i) eacc[i * 256 + t] = amode == 1 ? -acc[i] : acc[i];
+    }
+    __syncwarp();
+    const int cbase = n0 + half * 64;
+    const int* exBz = p.exB + (long long)zb * p.exB_stride;
+    const int ex_lo = cbase + lane < p.n ? exBz[cbase + lane] : 0;
+    const int ex_hi = cbase + 32 + lane < p.n ? exBz[cbase + 32 + lane] : 0;
+    // every lane runs the loop (the shuffles are warp-wide); lanes without an
+    // output (rows past m) only skip the loads and stores
+    const bool hi = p.D2 && r >= p.mD1;
+    const double* C = hi ? p.C2 + (long long)zb * p.sC - p.mD1
+                         : (p.C ? p.C + (long long)zb * p.sC : nullptr);
+    double* D = hi ? p.D2 + (long long)zb * p.sD - p.mD1 : p.D + (long long)zb * p.sD;
+    const int er = live ? p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1) + 2 : 0;
+    const bool use_c = p.betac != 0.0;
+    const double alpha = p.alpha, betac = p.betac;
+#pragma unroll 1
+    for (int i0 = 0; i0 < 64; i0 += 8) {
+      double cv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int c = cbase + i0 + q;
+        cv[q] = (live && use_c && c < p.n && !(p.outLower && r < c))
+                    ? C[(long long)r + (long long)c * p.ldc] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = i0 + q, c = cbase + i;
+        const int ec = __shfl_sync(0xffffffffu, i < 32 ? ex_lo : ex_hi, i & 31);
+        if (live && c < p.n && !(p.outLower && r < c)) {
+          double v = i64_ldexp(eacc[i * 256 + t], er + ec);
+          if (amode == 2) v *= alpha;
+          if (use_c) v = fma(betac, cv[q], v);
           D[(long long)r + (long long)c * p.ldd] = v;
         }
       }
