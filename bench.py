@@ -295,10 +295,11 @@ def run_batch(args):
         ms, launches, clk = timed()
         choices = {}
         for (s_, _, d_), t in zip(b.sizes, b.tunings()):
-            choices[f"ns{s_}_nd{d_}"] = [t["leaf_nb"], t["lookahead"], t["split_bias"]]
+            choices[f"ns{s_}_nd{d_}"] = [t["leaf_nb"], t["lookahead"], t["split_bias"],
+                                         t["splitk_max"], t["fp64_tile"]]
         tune = {"classes": classes, "tune_s": tune_s, "default_ms_per_step": ms_default,
                 "default_value": flops / (ms_default * 1e-3) / 1e12,
-                "choices_leaf_nb_lookahead_bias": choices}
+                "choices_leaf_nb_lookahead_bias_splitk_fp64tile": choices}
     # per-instance launches (each instance's own stage graphs, one after another)
     ms_serial = None
     if not args.no_per_instance:
@@ -368,7 +369,8 @@ def run_serve(args):
     nreq = args.serve_requests
     kinds0 = rng.choice([0, 1, 2], size=nreq, p=[0.7, 0.2, 0.1])
     kinds0[0] = 0
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=nreq))
+    rng_arrivals = np.random.default_rng(8)
+    arrivals = np.cumsum(rng_arrivals.exponential(1.0 / args.rate, size=nreq))
     mats0 = rng.integers(0, len(pool), size=nreq)
     nrhs = rng.integers(1, 17, size=nreq)
 
@@ -456,8 +458,23 @@ def run_serve(args):
                 "throughput_req_s": ok / makespan,
                 "fp64_equiv_tflops": flops / makespan / 1e12,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "by_kind": by, "evicted": stats["evicted"], "failed": stats["failed"]}, logdets
+                "by_kind": by, "evicted": stats["evicted"], "failed": stats["failed"],
+                "arena_fallbacks": stats["arena_fallbacks"]}, logdets
 
+    # latency below saturation: the same mix at a few lower offered rates
+    # (fewer requests each), chosen precision only
+    sweep = []
+    if args.serve_sweep:
+        saved = (args.rate, nreq)
+        for rate in [float(x) for x in args.serve_sweep.split(",")]:
+            nreq = args.serve_sweep_requests
+            arrivals = np.cumsum(np.random.default_rng(7).exponential(1.0 / rate, size=nreq))
+            r, _ = one_run(args.precision)
+            sweep.append({"rate_req_s": rate, "requests": nreq, "throughput_req_s": r["throughput_req_s"],
+                          "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "by_kind": r["by_kind"],
+                          "completed_ok": r["completed_ok"], "arena_fallbacks": r["arena_fallbacks"]})
+        args.rate, nreq = saved
+        arrivals = np.cumsum(rng_arrivals.exponential(1.0 / args.rate, size=nreq))
     split, ld_s = one_run(args.precision)
     plain, ld_p = one_run("fp64")
     common = [k for k in ld_s if k in ld_p]
@@ -474,6 +491,7 @@ def run_serve(args):
                        "nd_range": [0, 6], "matrix_pool": len(pool), "slots": args.serve_slots,
                        "hbm_budget_gb": args.serve_budget_gb},
             args.precision: split, "fp64": plain,
+            "below_saturation": sweep,
             "logdet_rel_err_split_vs_fp64": err}
     print(json.dumps(line), flush=True)
 
@@ -790,6 +808,10 @@ def main():
     p.add_argument("--serve-warm", type=int, default=8,
                    help="factors made resident before the request stream starts")
     p.add_argument("--serve-budget-gb", type=float, default=160.0)
+    p.add_argument("--serve-sweep", default="5,10,15",
+                   help="serve workload: offered rates (req/s) below saturation to report "
+                        "p50/p99 at, comma-separated ('' to skip)")
+    p.add_argument("--serve-sweep-requests", type=int, default=120)
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--no-per-instance", action="store_true",
                    help="batch workload: skip the instance-after-instance comparison run")

@@ -282,7 +282,11 @@ typedef struct rgf_tuning {
   double split_bias;
   double ms;        /* out: factorize + RGFdiag time measured by the autotuner
                        for this choice (0 when not measured)                 */
-  int reserved[4];
+  int splitk_max;   /* tile shapes: largest split-K degree of the tensor-core
+                       products (0 = default 16, 1 = no split K; 2, 4, 8)    */
+  int fp64_tile;    /* output tile of the FP64 products: 0 = chosen per
+                       product (32 or 64), 32 or 64 = always that           */
+  int reserved[2];
 } rgf_tuning;
 
 enum rgf_tune_flags {
@@ -350,10 +354,18 @@ typedef struct rgf_request {
 typedef struct rgf_server_stats_t {
   long long submitted, admitted, completed, failed, evicted;
   long long resident_factors, queued;
-  size_t used_bytes;
+  size_t used_bytes;        /* HBM reserved for admitted requests (estimates) */
+  size_t arena_bytes;       /* device memory pre-reserved at creation          */
+  size_t arena_in_use;      /* of which held by resident factors and requests  */
+  long long arena_fallbacks;/* allocations the arena could not serve (cudaMalloc) */
 } rgf_server_stats_t;
 
 typedef struct rgf_server rgf_server;
+/* The whole HBM budget is reserved at creation as one device arena: every
+ * handle a request creates takes its memory from it and eviction returns it
+ * there, so the steady state calls neither cudaMalloc nor cudaFree (whose
+ * device-wide wait would stall every request in flight).  RGF_ENOMEM if the
+ * budget cannot be reserved. */
 int rgf_server_create(const rgf_opts* opts, size_t hbm_budget_bytes, int slots,
                       rgf_server** out);
 int rgf_server_submit(rgf_server* s, rgf_request* req, long long* ticket);

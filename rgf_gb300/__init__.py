@@ -60,7 +60,8 @@ class _Request(C.Structure):
 
 class _Tuning(C.Structure):
     _fields_ = [("leaf_nb", C.c_int), ("lookahead", C.c_int), ("split_bias", C.c_double),
-                ("ms", C.c_double), ("reserved", C.c_int * 4)]
+                ("ms", C.c_double), ("splitk_max", C.c_int), ("fp64_tile", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 TUNE_FORCE = 1
@@ -68,12 +69,14 @@ TUNE_FORCE = 1
 
 def _tuning_dict(t: _Tuning) -> dict:
     return {"leaf_nb": t.leaf_nb, "lookahead": t.lookahead, "split_bias": t.split_bias,
-            "ms": t.ms}
+            "splitk_max": t.splitk_max, "fp64_tile": t.fp64_tile, "ms": t.ms}
 
 
-def _tuning_struct(leaf_nb: int, lookahead: int, split_bias: float) -> _Tuning:
+def _tuning_struct(leaf_nb: int, lookahead: int, split_bias: float, splitk_max: int = 0,
+                   fp64_tile: int = 0) -> _Tuning:
     t = _Tuning()
     t.leaf_nb, t.lookahead, t.split_bias = int(leaf_nb), int(lookahead), float(split_bias)
+    t.splitk_max, t.fp64_tile = int(splitk_max), int(fp64_tile)
     return t
 
 
@@ -81,7 +84,9 @@ class _ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong),
                 ("completed", C.c_longlong), ("failed", C.c_longlong),
                 ("evicted", C.c_longlong), ("resident_factors", C.c_longlong),
-                ("queued", C.c_longlong), ("used_bytes", C.c_size_t)]
+                ("queued", C.c_longlong), ("used_bytes", C.c_size_t),
+                ("arena_bytes", C.c_size_t), ("arena_in_use", C.c_size_t),
+                ("arena_fallbacks", C.c_longlong)]
 
 
 def library_path() -> str:
@@ -356,10 +361,12 @@ class RGF:
         autotuner's measured factorize + RGFdiag time ``ms`` (0 if none)."""
         return _tuning_of(self._lib, self._h)
 
-    def set_tuning(self, leaf_nb: int = 32, lookahead: int = 1, split_bias: float = 1.0) -> None:
+    def set_tuning(self, leaf_nb: int = 32, lookahead: int = 1, split_bias: float = 1.0,
+                   splitk_max: int = 0, fp64_tile: int = 0) -> None:
         """Set the knobs (leaf_nb 16/32/64, lookahead 0/1, split_bias in
-        [1/16, 16]); the factor is recomputed on next use."""
-        t = _tuning_struct(leaf_nb, lookahead, split_bias)
+        [1/16, 16], tile shapes: splitk_max 0/1/2/4/8/16 and fp64_tile
+        0/32/64); the factor is recomputed on next use."""
+        t = _tuning_struct(leaf_nb, lookahead, split_bias, splitk_max, fp64_tile)
         _check(self._lib.rgf_set_tuning(self._h, C.byref(t)), "rgf_set_tuning")
 
     def autotune(self, force: bool = False) -> dict:
@@ -492,9 +499,9 @@ class RGFBatch:
         return [_tuning_of(self._lib, self._handle(i)) for i in range(self.count)]
 
     def set_tuning(self, i: int, leaf_nb: int = 32, lookahead: int = 1,
-                   split_bias: float = 1.0) -> None:
+                   split_bias: float = 1.0, splitk_max: int = 0, fp64_tile: int = 0) -> None:
         """Set the knobs of instance i; the batch graph is captured again."""
-        t = _tuning_struct(leaf_nb, lookahead, split_bias)
+        t = _tuning_struct(leaf_nb, lookahead, split_bias, splitk_max, fp64_tile)
         _check(self._lib.rgf_set_tuning(self._handle(i), C.byref(t)), "rgf_set_tuning")
 
     def close(self) -> None:

@@ -575,7 +575,8 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
     return tiles;
   };
   const long long t64 = count_tiles(64);
-  const bool small = g.batch == 1 && g.ws && t64 * std::min(16, std::max(1, g.k / 16)) < 152;
+  const bool small = g.tile == 32 || (g.tile != 64 && g.batch == 1 && g.ws &&
+                                       t64 * std::min(16, std::max(1, g.k / 16)) < 152);
   const int tm = small ? 32 : 64, tk = small ? 8 : 16;
   const long long tiles = small ? count_tiles(32) : t64;
   // too few output tiles for 152 SMs (each SM retires only ~3.5 FP64 flops

@@ -1,5 +1,6 @@
 // Memory-bound kernels of the RGF recursion: CSC ingest into the block
 // layout, reductions, diagonal extraction, residual SpMV and small helpers.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -168,6 +169,43 @@ __global__ void sym_spmv_kernel(long long n, const size_t* __restrict__ ia,
   if (skipped && bad) atomicExch(bad, 1);
 }
 
+// Y[:, q] = A X[:, q] for q < nrhs (<= SPMV_MAX_RHS, columns n apart): the
+// product of sym_spmv_kernel for several right-hand sides in one pass over
+// the CSC (each entry is read once for all of them).  The CSC must be valid
+// (the handle's, which ingest checked).
+__global__ void sym_spmv_multi_kernel(long long n, const size_t* __restrict__ ia,
+                                      const size_t* __restrict__ ja,
+                                      const double* __restrict__ a,
+                                      const double* __restrict__ X, double* Y, int nrhs) {
+  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= n) return;
+  double xc[SPMV_MAX_RHS], g[SPMV_MAX_RHS];
+#pragma unroll
+  for (int q = 0; q < SPMV_MAX_RHS; ++q) {
+    xc[q] = q < nrhs ? X[q * n + c] : 0.0;
+    g[q] = 0.0;
+  }
+  for (size_t e = ia[c] + lane; e < ia[c + 1]; e += 32) {
+    const long long r = (long long)ja[e];
+    const double v = a[e];
+#pragma unroll
+    for (int q = 0; q < SPMV_MAX_RHS; ++q) {
+      if (q < nrhs) {
+        atomicAdd(&Y[q * n + r], v * xc[q]);
+        if (r != c) g[q] += v * X[q * n + r];
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < SPMV_MAX_RHS; ++q) {
+    double t = g[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0 && q < nrhs && t != 0.0) atomicAdd(&Y[q * n + c], t);
+  }
+}
+
 // out[0] = ||b - y||_2, out[1] = ||b||_2 (one CTA, 1024 threads).  As in
 // dnrm2, the sums of squares are scaled so that neither overflows nor
 // underflows: a first pass finds max |b - y| and max |b| (order-independent),
@@ -182,12 +220,14 @@ __device__ __forceinline__ double pow2_below_inv(double mx) {
 }
 
 __global__ void residual_norm_kernel(long long n, const double* b, const double* y, double* out,
-                                     const int* bad) {
+                                     const int* bad, const double* rres = nullptr) {
   __shared__ double s1[1024], s2[1024];
   const int t = threadIdx.x;
   double m1 = 0.0, m2 = 0.0;
+  // r_i = b_i - y_i, or rres[i] when the residual is given
+  auto res = [&](long long i) { return rres ? rres[i] : b[i] - y[i]; };
   for (long long i = t; i < n; i += blockDim.x) {
-    m1 = fmax(m1, fabs(b[i] - y[i]));
+    m1 = fmax(m1, fabs(res(i)));
     m2 = fmax(m2, fabs(b[i]));
   }
   s1[t] = m1;
@@ -206,7 +246,7 @@ __global__ void residual_norm_kernel(long long n, const double* b, const double*
   const double sr = fr ? pow2_below_inv(mr) : 1.0, sb = fb ? pow2_below_inv(mb) : 1.0;
   double r2 = 0.0, b2 = 0.0;
   for (long long i = t; i < n; i += blockDim.x) {
-    const double r = (b[i] - y[i]) * sr, bb = b[i] * sb;
+    const double r = res(i) * sr, bb = b[i] * sb;
     r2 += r * r;
     b2 += bb * bb;
   }
@@ -310,11 +350,18 @@ void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size
                              double* R, cudaStream_t s) {
   cudaMemsetAsync(Y, 0, sizeof(double) * n * nrhs, s);
   const long long threads = n * 32;
-  for (int q = 0; q < nrhs; ++q)
-    sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, X + q * n,
-                                                                      Y + q * n, nullptr);
+  const unsigned grid = (unsigned)((threads + 255) / 256);
+  for (int q0 = 0; q0 < nrhs; q0 += SPMV_MAX_RHS)  // the CSC is read once per 16 RHS
+    sym_spmv_multi_kernel<<<grid, 256, 0, s>>>(n, ia, ja, a, X + q0 * n, Y + q0 * n,
+                                               std::min(SPMV_MAX_RHS, nrhs - q0));
   const long long len = n * nrhs;
   sub_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, B, Y, R);
+}
+
+void launch_rhs_norms(long long n, int nrhs, const double* R, const double* B, double* out,
+                      cudaStream_t s) {
+  for (int q = 0; q < nrhs; ++q)
+    residual_norm_kernel<<<1, 1024, 0, s>>>(n, B + q * n, B + q * n, out + 2 * q, nullptr, R + q * n);
 }
 
 void launch_add(long long len, double* x, const double* d, cudaStream_t s) {

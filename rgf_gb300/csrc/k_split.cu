@@ -534,25 +534,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int er = live ? p.exA[(long long)zb * p.exA_stride + r] + p.cs - p.beta * (p.S + 1) + 2 : 0;
     const bool use_c = p.betac != 0.0;
     const double alpha = p.alpha, betac = p.betac;
+    // column pointers advance by ldc / ldd (no 64-bit multiply per output:
+    // on this GPU a wide integer multiply is as slow as an FP64 instruction)
+    const long long ldc = p.ldc, ldd = p.ldd;
+    const double* Cp = (live && use_c) ? C + r + (long long)cbase * ldc : nullptr;
+    double* Dp = live ? D + r + (long long)cbase * ldd : nullptr;
+    const int ncols = live ? min(64, p.n - cbase) : 0;          // columns < n
+    const int cdiag = p.outLower ? r - cbase : 64;                // columns c <= r only
+    const int nlive = max(0, min(ncols, cdiag + 1));
 #pragma unroll 1
     for (int i0 = 0; i0 < 64; i0 += 8) {
       double cv[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int c = cbase + i0 + q;
-        cv[q] = (live && use_c && c < p.n && !(p.outLower && r < c))
-                    ? C[(long long)r + (long long)c * p.ldc] : 0.0;
+        cv[q] = (Cp && i0 + q < nlive) ? *Cp : 0.0;
+        if (Cp) Cp += ldc;
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int i = i0 + q, c = cbase + i;
+        const int i = i0 + q;
         const int ec = __shfl_sync(0xffffffffu, i < 32 ? ex_lo : ex_hi, i & 31);
-        if (live && c < p.n && !(p.outLower && r < c)) {
+        if (i < nlive) {
           double v = i64_ldexp(eacc[i * 256 + t], er + ec);
           if (amode == 2) v *= alpha;
           if (use_c) v = fma(betac, cv[q], v);
-          D[(long long)r + (long long)c * p.ldd] = v;
+          *Dp = v;
         }
+        if (Dp) Dp += ldd;
       }
     }
   }
@@ -849,13 +857,13 @@ SplitEngine* SplitEngine::create(int slices, int* status) {
 }
 
 SplitEngine::~SplitEngine() {
-  if (ws_) cudaFree(ws_);
-  if (wsk_) cudaFree(wsk_);
+  device_free(ws_);
+  device_free(wsk_);
 }
 
-int SplitEngine::ensure_splitk(long long tiles) {
+int SplitEngine::ensure_splitk(long long tiles, cudaStream_t s) {
   if (tiles <= wsk_tiles_) return RGF_OK;
-  if (wsk_) cudaFree(wsk_);
+  device_free(wsk_);
   wsk_ = nullptr;
   cnt_ = nullptr;
   wsk_tiles_ = 0;
@@ -865,8 +873,8 @@ int SplitEngine::ensure_splitk(long long tiles) {
     cudaGetLastError();
     return RGF_ENOMEM;
   }
-  if (cudaMemset(p, 0, bytes) != cudaSuccess) {
-    cudaFree(p);
+  if (cudaMemsetAsync(p, 0, bytes, s) != cudaSuccess) {  // ordered before this stream's use
+    device_free(p);
     return RGF_ECUDA;
   }
   wsk_ = static_cast<long long*>(p);
@@ -884,7 +892,7 @@ int SplitEngine::reset_splitk(cudaStream_t s) {
 
 int SplitEngine::ensure_ws(size_t bytes) {
   if (bytes <= ws_bytes_) return RGF_OK;
-  if (ws_) cudaFree(ws_);
+  device_free(ws_);
   ws_ = nullptr;
   ws_bytes_ = 0;
   if (device_malloc(&ws_, bytes) != cudaSuccess) {
@@ -1014,7 +1022,8 @@ double SplitEngine::estimate_seconds(const GemmDesc& g, int slices) const {
   }
   long long ksplit = 1;
   if (wsk_ && tiles * 2 <= num_sms_ && (long long)tx * ty * g.batch <= wsk_tiles_)
-    ksplit = std::max<long long>(1, std::min<long long>({16, jobs, num_sms_ / std::max(1ll, tiles)}));
+    ksplit = std::max<long long>(
+        1, std::min<long long>({(long long)splitk_max_, jobs, num_sms_ / std::max(1ll, tiles)}));
   const double waves = std::ceil((double)(tiles * ksplit) / num_sms_);
   const bool same = g.A == g.B && g.lda == g.ldb && g.transA != g.transB;
   const double t_slice = (Kp <= SHORT_K ? 8e-6 : 16e-6) +
@@ -1033,7 +1042,7 @@ bool SplitEngine::supports(const GemmDesc& g) const {
          round_up(g.k, BKE) <= max_k_;
 }
 
-int SplitEngine::prepare(int max_rows, int max_k, int batch_hint) {
+int SplitEngine::prepare(int max_rows, int max_k, int batch_hint, cudaStream_t s) {
   max_rows_ = round_up(std::max(max_rows, 1), BM);
   max_k_ = round_up(std::max(max_k, 1), BKE);
   int dev = 0;
@@ -1045,7 +1054,7 @@ int SplitEngine::prepare(int max_rows, int max_k, int batch_hint) {
   int st = reserve(max_rows_, max_k_, batch_hint);
   if (st) return st;
   // split K serves launches whose tiles cover at most half of the SMs
-  return ensure_splitk(std::max(1, num_sms_ / 2));
+  return ensure_splitk(std::max(1, num_sms_ / 2), s);
 }
 
 long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
@@ -1175,7 +1184,7 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
     if (wsk_ && (long long)ntiles * nbat * 2 <= num_sms_ && grid_tiles <= wsk_tiles_) {
       int jobs = 0;  // jobs of a tile with the full K range
       for (int gi = 0; gi < p.ngroups; ++gi) jobs += (Kp / SBK + p.gchunk[gi] - 1) / p.gchunk[gi];
-      p.ksplit = std::max(1, std::min({16, jobs, num_sms_ / (ntiles * nbat)}));
+      p.ksplit = std::max(1, std::min({splitk_max_, jobs, num_sms_ / (ntiles * nbat)}));
     }
     p.wsk = wsk_;
     p.cnt = cnt_;

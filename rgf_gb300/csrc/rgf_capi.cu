@@ -31,7 +31,13 @@ using namespace rgf;
 
 namespace {
 constexpr int NB = 64;  // leaf tile of the FP64 panel Cholesky / triangular solves
-constexpr int RGF_REFINE_STEPS = 2;  // FP64 refinement steps of a split-precision solve
+// FP64 refinement of split-precision solves: at most this many correction
+// steps; refinement stops as soon as every right-hand side's normalized
+// residual ||b - A x|| / ||b|| is at or below RGF_REFINE_TOL (one step
+// suffices when the factor is accurate to ~1e-10: the error contracts by
+// about that factor per step)
+constexpr int RGF_REFINE_STEPS = 3;
+constexpr double RGF_REFINE_TOL = 1e-14;
 }
 
 struct rgf_handle {
@@ -72,6 +78,7 @@ struct rgf_handle {
   size_t partial_cap = 0;
   double* d_res = nullptr;      // residual scratch: x, b, y (3n)
   double* d_ref = nullptr;      // refinement of split solves: x, b, y (3 n nrhs)
+  double* d_norms = nullptr;    // refinement: ||r_q||, ||b_q|| per right-hand side (2 x 4096)
   size_t ref_cap = 0;           // doubles
   double* d_gemm_ws = nullptr;  // split-K partial sums of small FP64 GEMMs
   double* d_gemm_ws_side = nullptr;  // the same for the side stream
@@ -98,6 +105,8 @@ struct rgf_handle {
   int leaf_wait_polls = 0;   // poll limit of the leaf's pivot waits (0 = default)
   int nb = 32;               // leaf width of the panel Cholesky (16, 32 or 64)
   double split_bias = 1.0;   // the estimated split-product time is scaled by it
+  int splitk_max = 0;        // tile shapes: split-K cap of the tensor-core products (0 = 16)
+  int fp64_tile = 0;         // and the FP64 output tile (0 = per product)
   double tuned_ms = 0.0;     // factorize + RGFdiag time measured by the autotuner
   long long knob_gen = 0;
 
@@ -133,6 +142,110 @@ namespace rgf {
 // allocations left before the injected failure; < 0: injection off
 static std::atomic<long long> g_fail_alloc_after{-1};
 
+struct DeviceArena {
+  char* base = nullptr;
+  size_t size = 0;
+  std::mutex mu;
+  std::map<size_t, size_t> free_blocks;  // offset -> bytes
+  std::map<size_t, size_t> used_blocks;  // offset -> bytes
+  size_t in_use = 0;
+  long long fallbacks = 0;
+};
+
+static std::mutex g_arenas_mu;
+static std::vector<DeviceArena*> g_arenas;
+static thread_local DeviceArena* t_arena = nullptr;
+
+DeviceArena* arena_create(size_t bytes, int* status) {
+  *status = RGF_OK;
+  DeviceArena* a = new (std::nothrow) DeviceArena();
+  if (!a) {
+    *status = RGF_ENOMEM;
+    return nullptr;
+  }
+  bytes = (bytes + 255) & ~size_t(255);
+  if (cudaMalloc((void**)&a->base, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete a;
+    *status = RGF_ENOMEM;
+    return nullptr;
+  }
+  a->size = bytes;
+  a->free_blocks[0] = bytes;
+  std::lock_guard<std::mutex> lk(g_arenas_mu);
+  g_arenas.push_back(a);
+  return a;
+}
+
+void arena_destroy(DeviceArena* a) {
+  if (!a) return;
+  {
+    std::lock_guard<std::mutex> lk(g_arenas_mu);
+    g_arenas.erase(std::remove(g_arenas.begin(), g_arenas.end(), a), g_arenas.end());
+  }
+  cudaFree(a->base);
+  delete a;
+}
+
+void set_thread_arena(DeviceArena* a) { t_arena = a; }
+long long arena_fallbacks(DeviceArena* a) {
+  if (!a) return 0;
+  std::lock_guard<std::mutex> lk(a->mu);
+  return a->fallbacks;
+}
+size_t arena_in_use(DeviceArena* a) {
+  if (!a) return 0;
+  std::lock_guard<std::mutex> lk(a->mu);
+  return a->in_use;
+}
+
+static void* arena_alloc(DeviceArena* a, size_t bytes) {
+  bytes = (std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+  std::lock_guard<std::mutex> lk(a->mu);
+  for (auto it = a->free_blocks.begin(); it != a->free_blocks.end(); ++it) {
+    if (it->second < bytes) continue;
+    const size_t off = it->first, rest = it->second - bytes;
+    a->free_blocks.erase(it);
+    if (rest) a->free_blocks[off + bytes] = rest;
+    a->used_blocks[off] = bytes;
+    a->in_use += bytes;
+    return a->base + off;
+  }
+  a->fallbacks++;
+  return nullptr;
+}
+
+// true when p belonged to an arena (and is now free there)
+static bool arena_release(void* p) {
+  std::lock_guard<std::mutex> lk(g_arenas_mu);
+  for (DeviceArena* a : g_arenas) {
+    char* c = static_cast<char*>(p);
+    if (c < a->base || c >= a->base + a->size) continue;
+    std::lock_guard<std::mutex> la(a->mu);
+    size_t off = (size_t)(c - a->base);
+    auto u = a->used_blocks.find(off);
+    if (u == a->used_blocks.end()) return true;  // not a live block: ignore
+    size_t len = u->second;
+    a->used_blocks.erase(u);
+    a->in_use -= len;
+    auto next = a->free_blocks.lower_bound(off);
+    if (next != a->free_blocks.end() && next->first == off + len) {  // merge right
+      len += next->second;
+      next = a->free_blocks.erase(next);
+    }
+    if (next != a->free_blocks.begin()) {  // merge left
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        prev->second += len;
+        return true;
+      }
+    }
+    a->free_blocks[off] = len;
+    return true;
+  }
+  return false;
+}
+
 cudaError_t device_malloc(void** p, size_t bytes) {
   long long left = g_fail_alloc_after.load();
   while (left >= 0) {
@@ -144,7 +257,16 @@ cudaError_t device_malloc(void** p, size_t bytes) {
       break;
     }
   }
+  if (t_arena) {
+    *p = arena_alloc(t_arena, bytes);
+    if (*p) return cudaSuccess;
+  }
   return cudaMalloc(p, bytes);
+}
+
+void device_free(void* p) {
+  if (!p || arena_release(p)) return;
+  cudaFree(p);
 }
 }  // namespace rgf
 
@@ -183,9 +305,7 @@ int dalloc(rgf_handle* h, T** p, size_t count) {
   return RGF_OK;
 }
 
-void dfree(void* p) {
-  if (p) cudaFree(p);
-}
+void dfree(void* p) { device_free(p); }
 
 // ---- launch wrappers (count kernels; optional event timer on bulk GEMMs) ----
 // GEMM classes: SMALL always runs in FP64; BULK may run as split products;
@@ -276,6 +396,7 @@ void gemm(rgf_handle* h, const GemmDesc& g, int cls) {
     GemmDesc gw = g;
     gw.ws = h->on_side ? h->d_gemm_ws_side : h->d_gemm_ws;
     gw.ws_elems = h->gemm_ws_elems;
+    gw.tile = h->fp64_tile;
     launched = launch_gemm_fp64(gw, cur_stream(h));
   }
   h->kernels_issued += launched;
@@ -859,7 +980,8 @@ void release(rgf_handle* h) {
   delete h->split_side;
   void* bufs[] = {h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_MS, h->d_U, h->d_T1, h->d_T2, h->d_T3,
                   h->d_logpart, h->d_scalars, h->d_diag, h->d_status, h->d_rhs, h->d_partial,
-                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side, h->d_ref, h->d_rhs2};
+                  h->d_res, h->d_gemm_ws, h->d_gemm_ws_side, h->d_ref, h->d_rhs2,
+                  h->d_norms};
   for (void* p : bufs) dfree(p);
   if (h->side) cudaStreamSynchronize(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -996,11 +1118,11 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
       h->split = SplitEngine::create(o.slices, &st);
       if (st) break;
       // operands have at most 2ns+nd rows and ns+nd terms
-      st = h->split->prepare((int)(2 * ns + nd), (int)(ns + nd), (int)nt);
+      st = h->split->prepare((int)(2 * ns + nd), (int)(ns + nd), (int)nt, h->stream);
       if (st) break;
       h->split_side = SplitEngine::create(o.slices, &st);
       if (st) break;
-      st = h->split_side->prepare((int)(ns + nd), (int)ns, 1);
+      st = h->split_side->prepare((int)(ns + nd), (int)ns, 1, h->stream);
       if (st) break;
     }
     // validate the pattern once on the device
@@ -1152,9 +1274,12 @@ static int solve_real(rgf_handle* h, double* x, const double* b, size_t nrhs) {
     h->partial_cap = pneed;
   }
   // Split precision: the factor is accurate to ~1e-10, so the solve is
-  // refined in FP64 (RGF_REFINE_STEPS times): r = b - A x from the resident
-  // CSC, x += A~^{-1} r with the same factor.
+  // refined in FP64: r = b - A x from the resident CSC (one pass over it for
+  // up to 16 right-hand sides), and while some normalized residual is above
+  // RGF_REFINE_TOL, x += A~^{-1} r with the same factor (at most
+  // RGF_REFINE_STEPS times).
   const bool refine = h->opts.precision == RGF_PREC_SPLIT;
+  if (refine && !h->d_norms && (st = dalloc(h, &h->d_norms, 2 * 4096))) return st;
   if (refine && need * 3 > h->ref_cap) {
     dfree(h->d_ref);
     h->device_bytes -= h->ref_cap * sizeof(double);
@@ -1173,10 +1298,20 @@ static int solve_real(rgf_handle* h, double* x, const double* b, size_t nrhs) {
   cudaGraphExec_t exec = it == h->g_solve.end() ? nullptr : it->second.first;
   long long nk = it == h->g_solve.end() ? 0 : it->second.second;
   const int passes = refine ? 1 + RGF_REFINE_STEPS : 1;
+  std::vector<double> norms(refine ? 2 * nrhs : 0);
   for (int pass = 0; pass < passes; ++pass) {
-    if (pass > 0)  // d_rhs = b - A x
+    if (pass > 0) {  // d_rhs = b - A x; done when every residual is small
       launch_residual_vectors(n, (int)nrhs, h->d_ia, h->d_ja, h->d_a, xr, br, yr, h->d_rhs,
                               h->stream);
+      launch_rhs_norms(n, (int)nrhs, h->d_rhs, br, h->d_norms, h->stream);
+      RGF_CK(cudaMemcpyAsync(norms.data(), h->d_norms, sizeof(double) * 2 * nrhs,
+                             cudaMemcpyDeviceToHost, h->stream));
+      RGF_CK(cudaStreamSynchronize(h->stream));
+      bool done = true;
+      for (size_t q = 0; q < nrhs; ++q)
+        if (!(norms[2 * q] <= RGF_REFINE_TOL * norms[2 * q + 1])) done = false;
+      if (done) break;
+    }
     st = run_stage(h, &exec, &nk, &h->runs_solve[nrhs], [&] { issue_solve(h, (int)nrhs); });
     if (st) return st;
     if (exec) h->g_solve[nrhs] = {exec, nk};
@@ -1329,7 +1464,7 @@ int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m,
   SplitEngine* eng = nullptr;
   if (precision == RGF_PREC_SPLIT) {
     eng = SplitEngine::create(slices, &status);
-    if (!status) status = eng->prepare(std::max(m, n), k);
+    if (!status) status = eng->prepare(std::max(m, n), k, 1, s);
   }
   if (!status) {
     if (eng && eng->supports(g)) eng->gemm(g, s, st);
@@ -1577,7 +1712,10 @@ namespace {
 bool valid_tuning(const rgf_tuning& t) {
   return (t.leaf_nb == 16 || t.leaf_nb == 32 || t.leaf_nb == 64) &&
          (t.lookahead == 0 || t.lookahead == 1) && std::isfinite(t.split_bias) &&
-         t.split_bias >= 1.0 / 16 && t.split_bias <= 16.0;
+         t.split_bias >= 1.0 / 16 && t.split_bias <= 16.0 &&
+         (t.splitk_max == 0 || t.splitk_max == 1 || t.splitk_max == 2 || t.splitk_max == 4 ||
+          t.splitk_max == 8 || t.splitk_max == 16) &&
+         (t.fp64_tile == 0 || t.fp64_tile == 32 || t.fp64_tile == 64);
 }
 
 rgf_tuning knobs_of(const rgf_handle* h) {
@@ -1585,6 +1723,8 @@ rgf_tuning knobs_of(const rgf_handle* h) {
   t.leaf_nb = h->nb;
   t.lookahead = h->lookahead ? 1 : 0;
   t.split_bias = h->split_bias;
+  t.splitk_max = h->splitk_max;
+  t.fp64_tile = h->fp64_tile;
   t.ms = h->tuned_ms;
   return t;
 }
@@ -1595,6 +1735,10 @@ int set_knobs(rgf_handle* h, const rgf_tuning& t) {
   h->nb = t.leaf_nb;
   h->lookahead = t.lookahead != 0;
   h->split_bias = t.split_bias;
+  h->splitk_max = t.splitk_max;
+  h->fp64_tile = t.fp64_tile;
+  for (SplitEngine* e : {h->split, h->split_side})
+    if (e) e->set_splitk_max(t.splitk_max);
   h->tuned_ms = t.ms;
   h->knob_gen++;
   return RGF_OK;
@@ -1631,7 +1775,8 @@ int tune_handle(rgf_handle* h, rgf_tuning* out) {
   if ((st = time_factor_selinv(h, 2, &best.ms))) return st;
   auto trial = [&](rgf_tuning t) -> int {
     if (t.leaf_nb == best.leaf_nb && t.lookahead == best.lookahead &&
-        t.split_bias == best.split_bias)
+        t.split_bias == best.split_bias && t.splitk_max == best.splitk_max &&
+        t.fp64_tile == best.fp64_tile)
       return RGF_OK;
     int e = set_knobs(h, t);
     if (e) return e;
@@ -1655,6 +1800,16 @@ int tune_handle(rgf_handle* h, rgf_tuning* out) {
       t.split_bias = bias;
       if ((st = trial(t))) return st;
     }
+    for (int k : {1, 4}) {  // tile shapes: split-K degree of the tensor-core products
+      rgf_tuning t = best;
+      t.splitk_max = k;
+      if ((st = trial(t))) return st;
+    }
+  }
+  for (int tile : {32, 64}) {  // and the FP64 products' output tile
+    rgf_tuning t = best;
+    t.fp64_tile = tile;
+    if ((st = trial(t))) return st;
   }
   if ((st = set_knobs(h, best))) return st;
   *out = best;

@@ -47,6 +47,7 @@ struct GemmDesc {
   double* ws = nullptr;
   long long ws_elems = 0;
   int ksplit = 1;
+  int tile = 0;  // FP64 kernel: output tile 32 or 64; 0 = chosen by the launcher
 };
 
 // Algorithmic flops of one GemmDesc (triangular operands and lower-only
@@ -78,7 +79,22 @@ void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* s
 
 // Every device allocation of the library goes through here (so that a test
 // can make one fail: rgf_debug_fail_alloc_after).  cudaMalloc semantics.
+// On a thread that has a device arena set (set_thread_arena), memory comes
+// from the arena instead, with no cudaMalloc (and device_free returns it
+// there, with no cudaFree and its device-wide wait).
 cudaError_t device_malloc(void** p, size_t bytes);
+void device_free(void* p);
+
+// A device arena: one cudaMalloc of `bytes` at creation, then first-fit
+// sub-allocation (256-byte aligned, neighbours merged on free) under a mutex.
+// When it cannot serve a request (full or fragmented) device_malloc falls back
+// to cudaMalloc and counts it.
+struct DeviceArena;
+DeviceArena* arena_create(size_t bytes, int* status);
+void arena_destroy(DeviceArena* a);
+void set_thread_arena(DeviceArena* a);
+long long arena_fallbacks(DeviceArena* a);
+size_t arena_in_use(DeviceArena* a);
 
 // Row-parallel triangular solve with an nbk x nbk (nbk <= 64) lower tile L:
 //   mode 0: X := X * L^{-T}   (forward,  "R L T N")
@@ -130,6 +146,12 @@ cudaError_t launch_residual(long long n, const size_t* ia, const size_t* ja, con
 void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size_t* ja,
                              const double* a, const double* X, const double* B, double* Y,
                              double* R, cudaStream_t s);
+// out[2q] = ||R[:, q]||_2, out[2q + 1] = ||B[:, q]||_2 (columns n apart,
+// scaled sums of squares) for q < nrhs.
+void launch_rhs_norms(long long n, int nrhs, const double* R, const double* B, double* out,
+                      cudaStream_t s);
+// right-hand sides per pass of the multi-RHS SpMV of launch_residual_vectors
+constexpr int SPMV_MAX_RHS = 16;
 // x += d over len entries
 void launch_add(long long len, double* x, const double* d, cudaStream_t s);
 // out[q*ldo + dd] = sum_i sum_j C_i(dd, j) * R_i(j, q) over block columns,

@@ -19,11 +19,14 @@ class SplitEngine {
   // terms (allocates once, outside any graph capture).
   // batch_hint: largest batch the caller issues (sizes the workspace so that
   // batched problems run in few chunks; capped at 1 GiB).
-  int prepare(int max_rows, int max_k, int batch_hint = 1);
+  // The split-K workspace is cleared on stream s (before its first use there).
+  int prepare(int max_rows, int max_k, int batch_hint, cudaStream_t s);
   // True when g can run on the tensor cores (k >= min_k and within the
   // prepared sizes; batched problems run in chunks that fit the workspace).
   bool supports(const GemmDesc& g) const;
   int slices() const { return slices_; }
+  // Largest split-K degree (1 = none); a tuning knob.
+  void set_splitk_max(int k) { splitk_max_ = k > 0 ? k : 16; }
   // MMA streams per output tile and K term at S slices (each one N=256 MMA
   // of one A digit against two B digits, or N=128 against one)
   static int slots(int S);
@@ -43,7 +46,7 @@ class SplitEngine {
  private:
   SplitEngine() = default;
   int ensure_ws(size_t bytes);
-  int ensure_splitk(long long tiles);
+  int ensure_splitk(long long tiles, cudaStream_t s);
   int reserve(int max_rows, int max_k, int batch_hint);
   int slices_ = 0;
   int min_k_ = 1 << 30;
@@ -51,6 +54,7 @@ class SplitEngine {
   void* ws_ = nullptr;
   size_t ws_bytes_ = 0;
   int num_sms_ = 148;
+  int splitk_max_ = 16;
   // split K: int64 partial sums (128 x 128 per tile) and arrival counters
   long long* wsk_ = nullptr;
   int* cnt_ = nullptr;

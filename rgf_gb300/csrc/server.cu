@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/rgf.h"
+#include "rgf_internal.h"
 
 namespace {
 
@@ -54,6 +55,7 @@ size_t estimate_bytes(const rgf_opts& o, size_t ns, size_t nt, size_t nd, size_t
     b += std::max(one, std::min<size_t>((size_t)1 << 30, nt * one / 4)) + (1 << 20);
     const size_t r2 = (ns + nd + 127) / 128 * 128;
     b += 2 * 8 * r2 * k * 2 + (1 << 20);
+    b += 2 * (80 * 128 * 128 * 8 + 4096);  // split-K partial sums of both engines
   }
   return b + (8u << 20);
 }
@@ -72,6 +74,8 @@ struct rgf_server {
   bool stop = false;
   std::vector<std::thread> workers;
   rgf_server_stats_t stats{};
+  rgf::DeviceArena* arena = nullptr;  // the HBM budget, reserved once
+  int device = 0;
 };
 
 namespace {
@@ -188,6 +192,8 @@ void run_request(rgf_server* s, Pending p) {
 }
 
 void worker(rgf_server* s) {
+  cudaSetDevice(s->device);
+  rgf::set_thread_arena(s->arena);  // this thread's device memory comes from the arena
   std::unique_lock<std::mutex> lk(s->mu);
   while (true) {
     long i = -1;
@@ -216,6 +222,22 @@ int rgf_server_create(const rgf_opts* opts, size_t hbm_budget_bytes, int slots,
   rgf_default_opts(&s->opts);
   if (opts) s->opts = *opts;
   s->budget = hbm_budget_bytes;
+  int dev = s->opts.device;
+  if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) {
+    delete s;
+    return RGF_ECUDA;
+  }
+  if (cudaSetDevice(dev) != cudaSuccess) {
+    delete s;
+    return RGF_ECUDA;
+  }
+  s->device = dev;
+  int st = RGF_OK;
+  s->arena = rgf::arena_create(hbm_budget_bytes, &st);
+  if (st) {
+    delete s;
+    return st;
+  }
   for (int i = 0; i < slots; ++i) s->workers.emplace_back(worker, s);
   *out = s;
   return RGF_OK;
@@ -265,6 +287,9 @@ int rgf_server_stats(rgf_server* s, rgf_server_stats_t* out) {
   out->resident_factors = (long long)s->factors.size();
   out->used_bytes = s->used;
   out->queued = (long long)s->queue.size();
+  out->arena_bytes = s->budget;
+  out->arena_in_use = rgf::arena_in_use(s->arena);
+  out->arena_fallbacks = rgf::arena_fallbacks(s->arena);
   return RGF_OK;
 }
 
@@ -277,6 +302,7 @@ int rgf_server_destroy(rgf_server* s) {
   }
   for (auto& t : s->workers) t.join();
   for (auto& kv : s->factors) rgf_destroy(kv.second.h);
+  rgf::arena_destroy(s->arena);
   delete s;
   return RGF_OK;
 }

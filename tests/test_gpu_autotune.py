@@ -12,7 +12,7 @@ from rgf_gb300 import gen
 
 pytestmark = pytest.mark.gpu
 
-KNOBS = ("leaf_nb", "lookahead", "split_bias")
+KNOBS = ("leaf_nb", "lookahead", "split_bias", "splitk_max", "fp64_tile")
 
 
 def _knobs(t):
@@ -27,13 +27,13 @@ def test_every_knob_setting_matches_the_oracle(rgf, precision, ns, nt, nd, ltol,
     ia, ja, a = gen.generate_bta(ns, nt, nd, 11)
     ref = O.run_all(ns, nt, nd, ia, ja, a, exact=True)
     s = rgf.RGF(ia, ja, a, ns, nt, nd, precision=precision)
-    assert _knobs(s.tuning()) == (32, 1, 1.0)
+    assert _knobs(s.tuning()) == (32, 1, 1.0, 0, 0)
     biases = (0.5, 1.0, 2.0) if precision == "split" else (1.0,)
     for nb in (16, 32, 64):
         for la in (0, 1):
             for bias in biases:
                 s.set_tuning(nb, la, bias)
-                assert _knobs(s.tuning()) == (nb, la, bias)
+                assert _knobs(s.tuning()) == (nb, la, bias, 0, 0)
                 for _ in range(2):  # a direct run, then the captured graph
                     s.factorize()
                     ld, d = s.logDet(), s.RGFdiag()
@@ -42,15 +42,36 @@ def test_every_knob_setting_matches_the_oracle(rgf, precision, ns, nt, nd, ltol,
                         (nb, la, bias)
 
 
+@pytest.mark.parametrize("precision,ltol,dtol", [("fp64", 1e-12, 1e-10), ("split", 1e-9, 1e-8)])
+def test_tile_shape_knobs_match_the_oracle(rgf, precision, ltol, dtol):
+    """The autotuner's tile-shape knobs (split-K degree of the tensor-core
+    products, FP64 output tile) change how products are cut into CTAs (and,
+    through the cost model, which engine runs a product), never the results
+    beyond the precision's tolerance."""
+    ns, nt, nd = 520, 3, 4
+    ia, ja, a = gen.generate_bta(ns, nt, nd, seed=41)
+    ref = O.run_all(ns, nt, nd, ia, ja, a, exact=True)
+    s = rgf.RGF(ia, ja, a, ns, nt, nd, precision=precision)
+    for splitk in (1, 4, 0):
+        for tile in (0, 32, 64):
+            s.set_tuning(32, 1, 1.0, splitk, tile)
+            for _ in range(2):  # a direct run, then the captured graph
+                s.factorize()
+                ld, d = s.logDet(), s.RGFdiag()
+                assert abs(ld - ref["logdet"]) <= ltol * abs(ref["logdet"])
+                assert np.max(np.abs(d - ref["diag"]) / np.abs(ref["diag"])) <= dtol
+    s.close()
+
+
 def test_invalid_knobs_rejected(rgf):
     ia, ja, a = gen.generate_bta(20, 2, 1, 3)
     s = rgf.RGF(ia, ja, a, 20, 2, 1)
     for bad in ((8, 1, 1.0), (48, 1, 1.0), (32, 2, 1.0), (32, 1, 0.0), (32, 1, 100.0),
-                (32, 1, float("nan"))):
+                (32, 1, float("nan")), (32, 1, 1.0, 3, 0), (32, 1, 1.0, 0, 48)):
         with pytest.raises(rgf.RGFError) as e:
             s.set_tuning(*bad)
         assert e.value.status == 1
-    assert _knobs(s.tuning()) == (32, 1, 1.0)
+    assert _knobs(s.tuning()) == (32, 1, 1.0, 0, 0)
 
 
 def test_autotune_single_instance_and_cache(rgf):
@@ -82,7 +103,7 @@ def test_failed_autotune_leaves_knobs(rgf):
     with pytest.raises(rgf.RGFError) as e:
         s.autotune(force=True)
     assert e.value.status == 3
-    assert _knobs(s.tuning()) == (64, 0, 1.0)
+    assert _knobs(s.tuning()) == (64, 0, 1.0, 0, 0)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "split"])

@@ -53,6 +53,8 @@ def test_results_in_the_mix_equal_alone(rgf, precision):
         alone.close()
     st = srv.stats()
     assert st["completed"] == st["submitted"] == len(SHAPES) + len(jobs)
+    # every handle's device memory came from the pre-reserved arena
+    assert st["arena_bytes"] == 8 << 30 and st["arena_fallbacks"] == 0
     srv.close()
 
 
@@ -73,6 +75,8 @@ def test_eviction_and_release(rgf):
     assert ok["status"] == 0
     rel = srv.wait(srv.submit_release(f2["factor_id"]))
     assert rel["status"] == 0 and srv.stats()["resident_factors"] == 0
+    # eviction and release gave the memory back to the arena (no cudaFree)
+    assert srv.stats()["arena_in_use"] == 0
     srv.close()
 
 
