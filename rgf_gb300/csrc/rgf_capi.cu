@@ -1108,11 +1108,22 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
                                                            std::max<long long>(ns, nd));
     if ((st = dalloc(h, &h->d_gemm_ws, h->gemm_ws_elems))) break;
     if ((st = dalloc(h, &h->d_gemm_ws_side, h->gemm_ws_elems))) break;
-    if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice, h->stream) ||
-        cudaMemcpyAsync(h->d_ja, ja, sizeof(size_t) * h->nnz, cudaMemcpyHostToDevice, h->stream) ||
-        cudaMemcpyAsync(h->d_a, a, sizeof(double) * h->nnz, cudaMemcpyHostToDevice, h->stream)) {
-      st = RGF_ECUDA;
-      break;
+    // the CSC goes up in two halves on the two streams, so that two copy
+    // engines move it at once; the main stream joins before anything reads it
+    {
+      const size_t h1 = (size_t)h->nnz / 2, h2 = (size_t)h->nnz - h1;
+      if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice,
+                          h->stream) ||
+          cudaMemcpyAsync(h->d_ja, ja, sizeof(size_t) * h1, cudaMemcpyHostToDevice, h->stream) ||
+          cudaMemcpyAsync(h->d_a, a, sizeof(double) * h1, cudaMemcpyHostToDevice, h->stream) ||
+          cudaMemcpyAsync(h->d_ja + h1, ja + h1, sizeof(size_t) * h2, cudaMemcpyHostToDevice,
+                          h->side) ||
+          cudaMemcpyAsync(h->d_a + h1, a + h1, sizeof(double) * h2, cudaMemcpyHostToDevice,
+                          h->side)) {
+        st = RGF_ECUDA;
+        break;
+      }
+      join_side(h);
     }
     if (o.precision == RGF_PREC_SPLIT) {
       h->split = SplitEngine::create(o.slices, &st);
