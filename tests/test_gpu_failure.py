@@ -72,3 +72,24 @@ def test_failed_allocation_returns_enomem_and_releases(rgf, precision):
     tol = 1e-12 if precision == "fp64" else 1e-9
     assert abs(s.logDet() - ref["logdet"]) <= tol * abs(ref["logdet"])
     s.close()
+
+
+def test_launch_trace_records_every_launch(rgf, tmp_path, monkeypatch):
+    """RGF_GB300_TRACE=<file>: stages run launch by launch and every launch
+    leaves one CSV line (stage, index, stream, label, ms since the stage start),
+    with completion times in order on each stream; the results are unchanged."""
+    ns, nt, nd = 200, 3, 2
+    ia, ja, a = gen.generate_bta(ns, nt, nd, seed=33)
+    path = tmp_path / "trace.csv"
+    monkeypatch.setenv("RGF_GB300_TRACE", str(path))
+    s = rgf.RGF(ia, ja, a, ns, nt, nd, device=0)
+    monkeypatch.delenv("RGF_GB300_TRACE")
+    ld = s.logDet()
+    s.close()
+    rows = [ln.split(",") for ln in path.read_text().splitlines()]
+    assert len(rows) > 20 and {r[3] for r in rows} >= {"leaf", "ingest", "block end"}
+    for side in ("0", "1"):
+        t = [float(r[4]) for r in rows if r[0] == "0" and r[2] == side]
+        assert t == sorted(t)
+    ref = O.run_all(ns, nt, nd, ia, ja, a, exact=True)
+    assert abs(ld - ref["logdet"]) <= 1e-12 * abs(ref["logdet"])
