@@ -51,6 +51,10 @@ inline void env_opts(rgf_opts* o) {
   if (sel && std::strcmp(sel, "compat") == 0) o->selinv_mode = RGF_SELINV_COMPAT;
   const char* prec = std::getenv("RGF_GB300_PRECISION");
   if (prec && std::strcmp(prec, "split") == 0) o->precision = RGF_PREC_SPLIT;
+  // the reference keeps the caller's arrays (RGF.H:87-89), so the upload may
+  // overlap the first factorization; RGF_GB300_ASYNC_UPLOAD=0 copies at once
+  const char* up = std::getenv("RGF_GB300_ASYNC_UPLOAD");
+  o->async_upload = (up && up[0] == '0') ? 0 : 1;
 }
 }  // namespace rgf_gb300_detail
 

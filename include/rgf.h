@@ -56,7 +56,17 @@ typedef struct rgf_opts {
                        blocks: 1 (default) FP64 accuracy, their inner products
                        emulated with 7 slices (56-bit operands); 2 native FP64
                        units; 0 the bulk slice count                          */
-  int reserved[10];
+  int async_upload; /* 1: rgf_create queues the CSC upload and returns; the
+                       copies overlap the first factorization, which waits for
+                       each block column just before using it.  The caller's
+                       ia/ja/a must then stay valid and unchanged until the
+                       first call that factorizes (rgf_factorize / rgf_logdet /
+                       rgf_diag / rgf_solve) or rgf_residual_norm returns, or
+                       until rgf_destroy -- the reference's own contract
+                       (RGF.H:87-89 keeps the pointers), and pattern errors
+                       are reported by that call.  0 (default): copied and
+                       validated before rgf_create returns                    */
+  int reserved[9];
 } rgf_opts;
 
 typedef struct rgf_handle rgf_handle;
@@ -81,7 +91,8 @@ int rgf_default_opts(rgf_opts* opts);
 
 /* Replaces RGF<double>::RGF (RGF.H:84-146).  Validates the CSC against the
  * block-tridiagonal-arrowhead pattern and copies it to the device, so the
- * caller's arrays may be freed after the call.  opts may be NULL. */
+ * caller's arrays may be freed after the call (with opts->async_upload = 0,
+ * the default; see async_upload for the overlapped form).  opts may be NULL. */
 int rgf_create(const size_t* ia, const size_t* ja, const double* a,
                size_t ns, size_t nt, size_t nd,
                const rgf_opts* opts, rgf_handle** out);

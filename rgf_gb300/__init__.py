@@ -39,7 +39,7 @@ class RGFError(RuntimeError):
 class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("slices", C.c_int), ("selinv_mode", C.c_int),
                 ("device", C.c_int), ("use_graphs", C.c_int), ("fp64_diag", C.c_int),
-                ("reserved", C.c_int * 10)]
+                ("async_upload", C.c_int), ("reserved", C.c_int * 9)]
 
 
 class _Info(C.Structure):
@@ -232,15 +232,20 @@ class RGF:
     """Drop-in for the reference class ``RGF<double>`` (``RGF.H:11-80``).
 
     ``ia``/``ja`` are the column pointers and row indices (``size_t``) and
-    ``a`` the values of the matrix's lower triangle in CSC form.  Unlike the
-    reference, the arrays are copied to the device at construction.  A complex
+    ``a`` the values of the matrix's lower triangle in CSC form.  With
+    ``async_upload`` (the default) the copy to the device overlaps the first
+    factorization: the object keeps the arrays, as the reference keeps the
+    pointers (RGF.H:87-89), and they must not be changed until the first
+    factorize / logDet / RGFdiag / solve / residualNorm returns, which also
+    reports a CSC outside the block pattern.  ``async_upload=False`` copies
+    and validates them before the constructor returns.  A complex
     ``a`` makes a Hermitian instance (``RGF<complex<double>>``, RGF.H:756-774):
     logDet is then log det A and solve / RGFdiag take and return complex arrays.
     """
 
     def __init__(self, ia, ja, a, ns: int, nt: int, nd: int, precision: str = "fp64",
                  slices: int = 0, selinv: str = "exact", device: int = -1,
-                 use_graphs: bool = True, fp64_diag=1):
+                 use_graphs: bool = True, fp64_diag=1, async_upload: bool = True):
         lib = load_library()
         self._lib = lib
         self._h = C.c_void_p()
@@ -265,6 +270,7 @@ class RGF:
         # True/1: FP64-accurate emulated diagonal blocks, "native"/2: FP64
         # units, False/0: bulk slice count
         o.fp64_diag = {True: 1, False: 0, "native": 2}.get(fp64_diag, fp64_diag)
+        o.async_upload = 1 if async_upload else 0
         create = lib.rgf_create_hermitian if self.hermitian else lib.rgf_create
         _check(create(_ptr(self._ia), _ptr(self._ja), _ptr(self._a), self.ns, self.nt, self.nd,
                       C.byref(o), C.byref(self._h)), "rgf_create")

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
   constexpr int F = TM / 16;             // 8 x 8 fragments per warp side
   constexpr int LPT = TM * TK / 128;     // elements per thread per operand and stage
   constexpr int PAD = TM + 4;
+  pdl_wait();
   const int m0 = blockIdx.x * TM;
   const int n0 = blockIdx.y * TM;
   if (g.outLower && m0 + TM <= n0) return;  // tile entirely above the diagonal
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
       __syncthreads();
     }
   }
+  pdl_trigger();
 
   if (splitk) {  // raw partial sums of this K slice; reduced in fixed order later
     double* W = g.ws + (long long)blockIdx.z * g.m * g.n;
@@ -339,6 +341,7 @@ __device__ __forceinline__ void trsm_rows_body(double* X, long long xrs, long lo
       if (MODE == 0 ? (l > j && l < nbk) : (l < j)) u[t] = fma(-xj, MODE == 0 ? Ls[l][j] : Ls[j][l], u[t]);
     }
   }
+  pdl_trigger();
   if (live) {
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
@@ -358,6 +361,7 @@ __global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ld
   __shared__ double S[64][65];
   __shared__ int ready, abort_, fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  pdl_wait();
   for (int c = warp; c < nbk; c += 8)
     for (int r = c + lane; r < nbk; r += 32) S[r][c] = T[(long long)r + (long long)c * ldt];
   if (tid == 0) {
@@ -368,6 +372,7 @@ __global__ void __launch_bounds__(256) leaf_potrf_kernel(double* T, long long ld
   __syncthreads();
   leaf_chol(S, nbk, st, wait_polls, &ready, &abort_, &fail);
   __syncthreads();
+  pdl_trigger();
   for (int c = warp; c < nbk; c += 8)
     for (int r = c + lane; r < nbk; r += 32) T[(long long)r + (long long)c * ldt] = S[r][c];
   if (tid == 0 && fail != 0x7fffffff) atomicMin(&st->not_spd_col, col0 + fail);
@@ -382,6 +387,7 @@ __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs
                                                          int nbk, long long sX, long long sL) {
   __shared__ double Ls[64][65];
   __shared__ double rinv[64];
+  pdl_wait();
   X += (long long)blockIdx.y * sX;
   L += (long long)blockIdx.y * sL;
   for (int idx = threadIdx.x; idx < 64 * 64; idx += 128) {
@@ -401,6 +407,7 @@ __global__ void __launch_bounds__(128) trsm_rows_kernel(double* X, long long xrs
 // the split-K workspace in the GEMM kernel's layout.
 __global__ void __launch_bounds__(128) gemm_thin_m_kernel(GemmDesc g, int kchunk) {
   __shared__ double red[4][16][33];
+  pdl_wait();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + lane;
   const int k0 = blockIdx.y * kchunk, k1 = min(g.k, k0 + kchunk);
@@ -418,6 +425,7 @@ __global__ void __launch_bounds__(128) gemm_thin_m_kernel(GemmDesc g, int kchunk
         if (r < g.m) acc[r] = fma(g.transA ? a[(long long)r * g.lda] : a[r], b, acc[r]);
     }
   }
+  pdl_trigger();
 #pragma unroll
   for (int r = 0; r < 16; ++r) red[w][r][lane] = acc[r];
   __syncthreads();
@@ -439,6 +447,7 @@ __global__ void __launch_bounds__(128) gemm_thin_m_kernel(GemmDesc g, int kchunk
 __global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk) {
   __shared__ double As[32][129];
   __shared__ double Bs[32][17];
+  pdl_wait();
   const int tid = threadIdx.x;
   const int r0 = blockIdx.x * 128, r = r0 + tid;
   int k0 = blockIdx.y * kchunk, k1 = min(g.k, k0 + kchunk);
@@ -499,6 +508,7 @@ __global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk
       __syncthreads();
     }
   }
+  pdl_trigger();
   if (r < g.m) {
     double* W = g.ws + (long long)blockIdx.y * g.m * g.n;
 #pragma unroll
@@ -509,6 +519,8 @@ __global__ void __launch_bounds__(128) gemm_thin_n_kernel(GemmDesc g, int kchunk
 
 // D = alpha * sum_s W_s + beta * C over the split-K partials, in slice order.
 __global__ void splitk_reduce_kernel(GemmDesc g) {
+  pdl_wait();
+  pdl_trigger();
   const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
   if (r >= g.m || c >= g.n || (g.outLower && r < c)) return;
   const long long mn = (long long)g.m * g.n, o = (long long)r + (long long)c * g.m;
@@ -543,9 +555,9 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
     if ((long long)kchunks * g.m * g.n <= g.ws_elems) {
       const int kchunk = (g.k + kchunks - 1) / kchunks;
       g.ksplit = kchunks;
-      gemm_thin_m_kernel<<<dim3(cx, kchunks), 128, 0, s>>>(g, kchunk);
+      launch_k(gemm_thin_m_kernel, dim3(cx, kchunks), dim3(128), 0, s, g, kchunk);
       dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
-      splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
+      launch_k(splitk_reduce_kernel, rg, dim3(32, 8), 0, s, g);
       return 2;
     }
   }
@@ -559,9 +571,9 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
       const int kchunk = ((g.k + kchunks - 1) / kchunks + 31) / 32 * 32;
       kchunks = (g.k + kchunk - 1) / kchunk;
       g.ksplit = kchunks;
-      gemm_thin_n_kernel<<<dim3(rb, kchunks), 128, 0, s>>>(g, kchunk);
+      launch_k(gemm_thin_n_kernel, dim3(rb, kchunks), dim3(128), 0, s, g, kchunk);
       dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
-      splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
+      launch_k(splitk_reduce_kernel, rg, dim3(32, 8), 0, s, g);
       return 2;
     }
   }
@@ -592,11 +604,11 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
   g.ksplit = ksplit;
   const int tx = (g.m + tm - 1) / tm, ty = (g.n + tm - 1) / tm;
   dim3 grid(tx, ty, ksplit > 1 ? ksplit : g.batch);
-  if (small) gemm_fp64_kernel<32, 8><<<grid, 128, 0, s>>>(g);
-  else gemm_fp64_kernel<64, 16><<<grid, 128, 0, s>>>(g);
+  if (small) launch_k(gemm_fp64_kernel<32, 8>, grid, dim3(128), 0, s, g);
+  else launch_k(gemm_fp64_kernel<64, 16>, grid, dim3(128), 0, s, g);
   if (ksplit > 1) {
     dim3 rg((g.m + 31) / 32, (g.n + 7) / 8);
-    splitk_reduce_kernel<<<rg, dim3(32, 8), 0, s>>>(g);
+    launch_k(splitk_reduce_kernel, rg, dim3(32, 8), 0, s, g);
     return 2;
   }
   return 1;
@@ -605,8 +617,8 @@ int launch_gemm_fp64(const GemmDesc& g0, cudaStream_t s) {
 void launch_leaf_potrf(double* T, long long ldt, int nbk, int col0, DevStatus* st,
                        cudaStream_t s, int wait_polls) {
   if (nbk <= 0) return;
-  leaf_potrf_kernel<<<1, 256, 0, s>>>(T, ldt, nbk, col0, st,
-                                      wait_polls > 0 ? wait_polls : LEAF_WAIT_POLLS);
+  launch_k(leaf_potrf_kernel, dim3(1), dim3(256), 0, s, T, ldt, nbk, col0, st,
+           wait_polls > 0 ? wait_polls : LEAF_WAIT_POLLS);
 }
 
 void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const double* L,
@@ -615,9 +627,9 @@ void launch_trsm_rows(double* X, long long xrs, long long xcs, int rows, const d
   if (rows <= 0 || nbk <= 0 || batch <= 0) return;
   dim3 grid((rows + 15) / 16, batch);
   if (mode == 0)
-    trsm_rows_kernel<0><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+    launch_k(trsm_rows_kernel<0>, grid, dim3(128), 0, s, X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
   else
-    trsm_rows_kernel<1><<<grid, 128, 0, s>>>(X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
+    launch_k(trsm_rows_kernel<1>, grid, dim3(128), 0, s, X, xrs, xcs, rows, L, ldl, nbk, sX, sL);
 }
 
 }  // namespace rgf

@@ -37,12 +37,15 @@ namespace {
 // computed once, then every entry maps to a row of that panel.  Follows the
 // mapping of the reference's getPos (CWC_utility.cu:998-1029) without its
 // per-entry linear column search (CWC_utility.cu:1093-1095).
-__global__ void ingest_kernel(BtaShape sh, const size_t* __restrict__ ia,
-                              const size_t* __restrict__ ja, const double* __restrict__ a,
-                              double* __restrict__ MF, DevStatus* st) {
-  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void ingest_kernel(BtaShape sh, long long c_lo, long long c_hi,
+                              const size_t* __restrict__ ia, const size_t* __restrict__ ja,
+                              const double* __restrict__ a, double* __restrict__ MF,
+                              DevStatus* st) {
+  pdl_wait();
+  pdl_trigger();
+  const long long c = c_lo + (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (c >= sh.n) return;
+  if (c >= c_hi) return;
   const long long ns = sh.ns, nt = sh.nt, nd = sh.nd, n = sh.n;
   const long long ib = c < ns * nt ? c / ns : nt;
   const long long jc = ib < nt ? c - ib * ns : c - nt * ns;
@@ -71,6 +74,8 @@ __global__ void ingest_kernel(BtaShape sh, const size_t* __restrict__ ia,
 // log of every diagonal entry of the factor MF; each block of 256 columns sums
 // its logs in a fixed tree order into parts[block]
 __global__ void diag_log_kernel(BtaShape sh, const double* MF, double* parts) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double v[256];
   const long long k = (long long)blockIdx.x * 256 + threadIdx.x;
   double x = 0.0;
@@ -96,6 +101,8 @@ __global__ void diag_log_kernel(BtaShape sh, const double* MF, double* parts) {
 }
 
 __global__ void logdet_reduce_kernel(const double* parts, int nparts, double* out) {
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x;
   double s = 0.0;
   for (int i = lane; i < nparts; i += 32) s += parts[i];
@@ -110,6 +117,8 @@ __global__ void logdet_reduce_kernel(const double* parts, int nparts, double* ou
 }
 
 __global__ void extract_diag_kernel(BtaShape sh, const double* MS, double* diag) {
+  pdl_wait();
+  pdl_trigger();
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sh.n) return;
   const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
@@ -125,6 +134,8 @@ __global__ void extract_diag_kernel(BtaShape sh, const double* MS, double* diag)
 }
 
 __global__ void set_identity_kernel(double* X, long long ld, int m, long long stride) {
+  pdl_wait();
+  pdl_trigger();
   X += (long long)blockIdx.z * stride;
   const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
   if (r < m && c < m) X[r + (long long)c * ld] = (r == c) ? 1.0 : 0.0;
@@ -132,6 +143,8 @@ __global__ void set_identity_kernel(double* X, long long ld, int m, long long st
 
 __global__ void copy_kernel(const double* X, long long ldx, double* Y, long long ldy, int m,
                             int n, long long sX, long long sY) {
+  pdl_wait();
+  pdl_trigger();
   X += (long long)blockIdx.z * sX;
   Y += (long long)blockIdx.z * sY;
   const int r = blockIdx.x * 32 + threadIdx.x, c = blockIdx.y * 8 + threadIdx.y;
@@ -146,6 +159,8 @@ __global__ void copy_kernel(const double* X, long long ldx, double* Y, long long
 __global__ void sym_spmv_kernel(long long n, const size_t* __restrict__ ia,
                                 const size_t* __restrict__ ja, const double* __restrict__ a,
                                 const double* __restrict__ x, double* y, int* bad) {
+  pdl_wait();
+  pdl_trigger();
   const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= n) return;
@@ -177,6 +192,8 @@ __global__ void sym_spmv_multi_kernel(long long n, const size_t* __restrict__ ia
                                       const size_t* __restrict__ ja,
                                       const double* __restrict__ a,
                                       const double* __restrict__ X, double* Y, int nrhs) {
+  pdl_wait();
+  pdl_trigger();
   const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= n) return;
@@ -221,6 +238,8 @@ __device__ __forceinline__ double pow2_below_inv(double mx) {
 
 __global__ void residual_norm_kernel(long long n, const double* b, const double* y, double* out,
                                      const int* bad, const double* rres = nullptr) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double s1[1024], s2[1024];
   const int t = threadIdx.x;
   double m1 = 0.0, m2 = 0.0;
@@ -272,6 +291,8 @@ __global__ void residual_norm_kernel(long long n, const double* b, const double*
 // column i, one warp per (dd, q) pair, fixed-order warp reduction.
 __global__ void arrow_gemv_kernel(BtaShape sh, const double* MF, const double* rhs, long long ldr,
                                   int nrhs, double* partial) {
+  pdl_wait();
+  pdl_trigger();
   const long long i = blockIdx.x;
   const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
   const double* Cb = MF + col_offset_d(ns, nt, nd, i) + dense_row_d(ns, nt, i);
@@ -290,6 +311,8 @@ __global__ void arrow_gemv_kernel(BtaShape sh, const double* MF, const double* r
 
 __global__ void arrow_reduce_kernel(BtaShape sh, const double* partial, int nrhs, double* rhs,
                                     long long ldr) {
+  pdl_wait();
+  pdl_trigger();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const long long nd = sh.nd;
   if (p >= nd * nrhs) return;
@@ -302,10 +325,13 @@ __global__ void arrow_reduce_kernel(BtaShape sh, const double* partial, int nrhs
 }  // namespace
 
 void launch_ingest(const BtaShape& sh, const size_t* ia, const size_t* ja, const double* a,
-                   double* MF, DevStatus* st, cudaStream_t s) {
-  const long long threads = sh.n * 32;
+                   double* MF, DevStatus* st, cudaStream_t s, long long c_lo, long long c_hi) {
+  if (c_hi < 0) c_hi = sh.n;
+  if (c_hi <= c_lo) return;
+  const long long threads = (c_hi - c_lo) * 32;
   const int bs = 256;
-  ingest_kernel<<<(unsigned)((threads + bs - 1) / bs), bs, 0, s>>>(sh, ia, ja, a, MF, st);
+  launch_k(ingest_kernel, dim3((unsigned)((threads + bs - 1) / bs)), dim3(bs), 0, s, sh, c_lo,
+           c_hi, ia, ja, a, MF, st);
 }
 
 int logdet_parts(const BtaShape& sh) { return (int)((sh.n + 255) / 256); }
@@ -313,34 +339,39 @@ int logdet_parts(const BtaShape& sh) { return (int)((sh.n + 255) / 256); }
 void launch_logdet(const BtaShape& sh, const double* MF, double* parts, double* out,
                    cudaStream_t s) {
   const int np = logdet_parts(sh);
-  diag_log_kernel<<<np, 256, 0, s>>>(sh, MF, parts);
-  logdet_reduce_kernel<<<1, 32, 0, s>>>(parts, np, out);
+  launch_k(diag_log_kernel, dim3(np), dim3(256), 0, s, sh, MF, parts);
+  launch_k(logdet_reduce_kernel, dim3(1), dim3(32), 0, s, parts, np, out);
 }
 
 void launch_extract_diag(const BtaShape& sh, const double* MS, double* diag, cudaStream_t s) {
-  extract_diag_kernel<<<(unsigned)((sh.n + 255) / 256), 256, 0, s>>>(sh, MS, diag);
+  launch_k(extract_diag_kernel, dim3((unsigned)((sh.n + 255) / 256)), dim3(256), 0, s, sh, MS,
+           diag);
 }
 
 void launch_set_identity(double* X, long long ld, int m, int batch, long long stride,
                          cudaStream_t s) {
   if (m <= 0 || batch <= 0) return;
   dim3 grid((m + 31) / 32, (m + 7) / 8, batch);
-  set_identity_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ld, m, stride);
+  launch_k(set_identity_kernel, grid, dim3(32, 8), 0, s, X, ld, m, stride);
 }
 
 void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,
                  int batch, long long sX, long long sY, cudaStream_t s) {
   if (m <= 0 || n <= 0 || batch <= 0) return;
   dim3 grid((m + 31) / 32, (n + 7) / 8, batch);
-  copy_kernel<<<grid, dim3(32, 8), 0, s>>>(X, ldx, Y, ldy, m, n, sX, sY);
+  launch_k(copy_kernel, grid, dim3(32, 8), 0, s, X, ldx, Y, ldy, m, n, sX, sY);
 }
 
 // r = b - y; x += d (element-wise over len entries)
 __global__ void sub_kernel(long long len, const double* b, const double* y, double* r) {
+  pdl_wait();
+  pdl_trigger();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < len) r[i] = b[i] - y[i];
 }
 __global__ void add_kernel(long long len, double* x, const double* d) {
+  pdl_wait();
+  pdl_trigger();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < len) x[i] += d[i];
 }
@@ -352,20 +383,21 @@ void launch_residual_vectors(long long n, int nrhs, const size_t* ia, const size
   const long long threads = n * 32;
   const unsigned grid = (unsigned)((threads + 255) / 256);
   for (int q0 = 0; q0 < nrhs; q0 += SPMV_MAX_RHS)  // the CSC is read once per 16 RHS
-    sym_spmv_multi_kernel<<<grid, 256, 0, s>>>(n, ia, ja, a, X + q0 * n, Y + q0 * n,
-                                               std::min(SPMV_MAX_RHS, nrhs - q0));
+    launch_k(sym_spmv_multi_kernel, dim3(grid), dim3(256), 0, s, n, ia, ja, a, X + q0 * n,
+             Y + q0 * n, std::min(SPMV_MAX_RHS, nrhs - q0));
   const long long len = n * nrhs;
-  sub_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, B, Y, R);
+  launch_k(sub_kernel, dim3((unsigned)((len + 255) / 256)), dim3(256), 0, s, len, B, Y, R);
 }
 
 void launch_rhs_norms(long long n, int nrhs, const double* R, const double* B, double* out,
                       cudaStream_t s) {
   for (int q = 0; q < nrhs; ++q)
-    residual_norm_kernel<<<1, 1024, 0, s>>>(n, B + q * n, B + q * n, out + 2 * q, nullptr, R + q * n);
+    launch_k(residual_norm_kernel, dim3(1), dim3(1024), 0, s, n, B + q * n, B + q * n, out + 2 * q,
+             (const int*)nullptr, (const double*)(R + q * n));
 }
 
 void launch_add(long long len, double* x, const double* d, cudaStream_t s) {
-  add_kernel<<<(unsigned)((len + 255) / 256), 256, 0, s>>>(len, x, d);
+  launch_k(add_kernel, dim3((unsigned)((len + 255) / 256)), dim3(256), 0, s, len, x, d);
 }
 
 cudaError_t launch_residual(long long n, const size_t* ia, const size_t* ja, const double* a,
@@ -375,22 +407,25 @@ cudaError_t launch_residual(long long n, const size_t* ia, const size_t* ja, con
   if (e == cudaSuccess && bad) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   const long long threads = n * 32;
-  sym_spmv_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, ia, ja, a, x, scratch, bad);
-  residual_norm_kernel<<<1, 1024, 0, s>>>(n, b, scratch, out, bad);
+  launch_k(sym_spmv_kernel, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, s, n, ia, ja,
+           a, x, scratch, bad);
+  launch_k(residual_norm_kernel, dim3(1), dim3(1024), 0, s, n, b, (const double*)scratch, out,
+           (const int*)bad, (const double*)nullptr);
   return cudaGetLastError();
 }
 
 void launch_arrow_gemv(const BtaShape& sh, const double* MF, const double* rhs, long long ldr,
                        int nrhs, double* partial, cudaStream_t s) {
   if (sh.nd <= 0) return;
-  arrow_gemv_kernel<<<(unsigned)sh.nt, 256, 0, s>>>(sh, MF, rhs, ldr, nrhs, partial);
+  launch_k(arrow_gemv_kernel, dim3((unsigned)sh.nt), dim3(256), 0, s, sh, MF, rhs, ldr, nrhs,
+           partial);
 }
 
 void launch_arrow_reduce(const BtaShape& sh, const double* partial, int nrhs, double* rhs,
                          long long ldr, cudaStream_t s) {
   if (sh.nd <= 0) return;
   const int p = (int)(sh.nd * nrhs);
-  arrow_reduce_kernel<<<(p + 127) / 128, 128, 0, s>>>(sh, partial, nrhs, rhs, ldr);
+  launch_k(arrow_reduce_kernel, dim3((p + 127) / 128), dim3(128), 0, s, sh, partial, nrhs, rhs, ldr);
 }
 
 }  // namespace rgf

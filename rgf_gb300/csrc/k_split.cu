@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  pdl_wait();  // the setup above overlaps the previous kernel's tail
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -475,6 +476,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
+    pdl_trigger();  // the products are done: the next kernel may be scheduled
     if (p.ksplit > 1) {
       // split K: add this slice's partial sums to the tile's workspace; the
       // last slice to arrive takes the total (and leaves zeros behind)
@@ -621,6 +623,8 @@ __device__ __forceinline__ int exp_of_max(unsigned long long mx) {
 __global__ void rowmax_rowmajor_kernel(const double* X, long long ks, int R, int K, int tri,
                                        unsigned long long* mx, long long sX, int Rp,
                                        const double* X2, int R1) {
+  pdl_wait();
+  pdl_trigger();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
   X = (X2 && r >= R1 ? X2 - R1 : X) + (long long)blockIdx.z * sX;
@@ -639,6 +643,8 @@ __global__ void rowmax_rowmajor_kernel(const double* X, long long ks, int R, int
 // k contiguous (ks == 1): one warp per row
 __global__ void rowmax_kmajor_kernel(const double* X, long long rs, int R, int K, int tri,
                                      unsigned long long* mx, int Rp, long long sX) {
+  pdl_wait();
+  pdl_trigger();
   const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (r >= Rp) return;
   X += (long long)blockIdx.y * sX;
@@ -661,6 +667,8 @@ __global__ void rowmax_kmajor_kernel(const double* X, long long rs, int R, int K
 }
 
 __global__ void row_exp_kernel(const unsigned long long* mx, int* ex, int Rp) {
+  pdl_wait();
+  pdl_trigger();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const long long o = (long long)blockIdx.y * Rp;
   if (r < Rp) ex[o + r] = exp_of_max(mx[o + r]);
@@ -673,6 +681,8 @@ __global__ void slice_kernel(const double* X, long long rs, long long ks, int R,
                              const int* ex, __nv_bfloat16* out, int Rp, int Kp, int S, int beta,
                              long long sX, const double* X2, int R1) {
   __shared__ double tile[32][33];
+  pdl_wait();
+  pdl_trigger();
   X += (long long)blockIdx.z * sX;
   const double* Xb = X2 ? X2 - R1 + (long long)blockIdx.z * sX : X;
   ex += (long long)blockIdx.z * Rp;
@@ -721,6 +731,8 @@ __global__ void __launch_bounds__(256) slice_pair_kernel(SliceOperand a, SliceOp
                                                           int K, int Kp, int S, int beta) {
   __shared__ double tile[32][33];
   __shared__ unsigned long long red[8][33];
+  pdl_wait();
+  pdl_trigger();
   const bool isA = (int)blockIdx.x < nblkA;
   const SliceOperand& o = isA ? a : b;
   const int r0 = (isA ? blockIdx.x : blockIdx.x - nblkA) * 32;
@@ -1032,6 +1044,23 @@ double SplitEngine::estimate_seconds(const GemmDesc& g, int slices) const {
   return 20e-6 + t_slice + waves * steps * 120e-9;
 }
 
+// Tensor maps are encoded once per (base, planes, rows, K) and reused: the
+// workspace base is fixed per engine, so a handle's products need only a few
+// distinct maps, and the driver call is a noticeable part of a product's host
+// cost when stages are launched directly.
+bool SplitEngine::map_for(CUtensorMap* out, void* base, int S, int Rp, int Kp) {
+  const auto key = std::make_tuple(base, S, Rp, Kp);
+  auto it = maps_.find(key);
+  if (it != maps_.end()) {
+    *out = it->second;
+    return true;
+  }
+  if (!make_map(out, base, S, Rp, Kp)) return false;
+  if (maps_.size() >= 512) maps_.clear();
+  maps_.emplace(key, *out);
+  return true;
+}
+
 int SplitEngine::slots(int S) {
   return S >= 1 && S <= MAX_SLICES ? (int)slot_plan(S).slots.size() : 0;
 }
@@ -1121,15 +1150,17 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       if (rs == 1) {
         cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rp * nbat, s);
         dim3 grid((R + 127) / 128, (g.k + 31) / 32, nbat);
-        rowmax_rowmajor_kernel<<<grid, 128, 0, s>>>(X, ks, R, g.k, tri, mx, sX, Rp, X2, R1);
+        launch_k(rowmax_rowmajor_kernel, grid, dim3(128), 0, s, X, ks, R, (int)g.k, tri, mx, sX,
+                 Rp, X2, R1);
       } else {
         dim3 grid((Rp * 32 + 255) / 256, nbat);
-        rowmax_kmajor_kernel<<<grid, 256, 0, s>>>(X, rs, R, g.k, tri, mx, Rp, sX);
+        launch_k(rowmax_kmajor_kernel, grid, dim3(256), 0, s, X, rs, R, (int)g.k, tri, mx, Rp, sX);
       }
-      row_exp_kernel<<<dim3((Rp + 255) / 256, nbat), 256, 0, s>>>(mx, ex, Rp);
+      launch_k(row_exp_kernel, dim3((Rp + 255) / 256, nbat), dim3(256), 0, s,
+               (const unsigned long long*)mx, ex, Rp);
       dim3 grid(Kp / 32, Rp / 32, nbat);
-      slice_kernel<<<grid, dim3(32, 8), 0, s>>>(X, rs, ks, R, g.k, tri, ex, out, Rp, Kp, S, beta,
-                                                sX, X2, R1);
+      launch_k(slice_kernel, grid, dim3(32, 8), 0, s, X, rs, ks, R, (int)g.k, tri,
+               (const int*)ex, out, Rp, Kp, S, beta, sX, X2, R1);
       launched += 3;
     };
     const double* A = g.A + (long long)b0 * g.sA;
@@ -1141,8 +1172,8 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       SliceOperand ob{B, nullptr, g.transB ? 1 : g.ldb, g.transB ? g.ldb : 1, g.sB, g.n, g.n,
                       RpB, triBt, exB, sb};
       const int nblkA = RpA / 32, nblkB = same ? 0 : RpB / 32;
-      slice_pair_kernel<<<dim3(nblkA + nblkB, (Kp + SLICE_KC - 1) / SLICE_KC, nbat), 256, 0, s>>>(
-          oa, ob, nblkA, g.k, Kp, S, beta);
+      launch_k(slice_pair_kernel, dim3(nblkA + nblkB, (Kp + SLICE_KC - 1) / SLICE_KC, nbat),
+               dim3(256), 0, s, oa, ob, nblkA, (int)g.k, Kp, S, beta);
       launched += 1;
     } else {
       if (!g.transA) slice(A, 1, g.lda, g.sA, g.m, g.triA, exA, mxA, sa, RpA, A2, g.mA1);
@@ -1153,8 +1184,8 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
       }
     }
     CUtensorMap ma, mb;
-    if (!make_map(&ma, sa, S * nbat, RpA, Kp) ||
-        !make_map(&mb, sb, S * nbat, same ? RpA : RpB, Kp)) {
+    if (!map_for(&ma, sa, S * nbat, RpA, Kp) ||
+        !map_for(&mb, sb, S * nbat, same ? RpA : RpB, Kp)) {
       GemmDesc f = g;  // cannot describe the operands: FP64 kernel for this chunk
       f.batch = nbat;
       f.A = A; f.B = g.B + (long long)b0 * g.sB;
@@ -1196,7 +1227,7 @@ long long SplitEngine::gemm(const GemmDesc& g, cudaStream_t s, DevStatus* st,
           if (!(g.outLower && bx * BM + BM <= by * BN)) tiles += 1.0;
       *tensor_flops += tiles * nbat * 2.0 * BM * BN * (double)round_up(Kp, SBK) * np;
     }
-    split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, p);
+    launch_k(split_gemm_kernel, grid, dim3(NUM_THREADS), SMEM_BYTES, s, ma, mb, p);
     launched += 1;
   }
   return launched;

@@ -94,6 +94,14 @@ struct rgf_handle {
   long long k_factor = 0, k_selinv = 0, k_inv = 0;
   std::map<size_t, std::pair<cudaGraphExec_t, long long>> g_solve;
   int runs_factor = 0, runs_selinv = 0, runs_inv = 0;  // stage runs so far (the first is not captured)
+  bool mf_holds_a = false;  // MF holds the ingested A (create's validation), not yet factored
+  // Asynchronous upload (rgf_opts.async_upload): create queues the CSC copies
+  // and the ingest of every block column on `upload` and returns; ev_chunk[i]
+  // marks block column i of MF holding A (i = nt: the arrowhead corner).  The
+  // first factorization waits for each block column just before using it.
+  cudaStream_t upload = nullptr;
+  std::vector<cudaEvent_t> ev_chunk;
+  bool upload_pending = false;
   std::map<size_t, int> runs_solve;
   long long kernels_issued = 0;   // kernels of the stage being recorded
   long long kernels_total = 0;    // kernels launched over the handle's life
@@ -244,6 +252,14 @@ static bool arena_release(void* p) {
     return true;
   }
   return false;
+}
+
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("RGF_GB300_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
 }
 
 cudaError_t device_malloc(void** p, size_t bytes) {
@@ -500,15 +516,35 @@ void issue_factor(rgf_handle* h) {
   const BtaShape& sh = h->sh;
   const long long ns = sh.ns, nt = sh.nt, nd = sh.nd;
   cudaStream_t s = h->stream;
-  status_init_kernel<<<1, 1, 0, s>>>(h->d_status);
-  cudaMemsetAsync(h->d_MF, 0, sizeof(double) * h->mf_size, s);
-  launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, s);
-  h->kernels_issued += 2;
-  trace(h, "ingest");
+  // first factorization after an asynchronous create: block column i is
+  // waited for just before its first use (the corner, uploaded first, now);
+  // the status was initialized before the uploads' ingests, which record
+  // pattern errors in it
+  const bool streamed = h->upload_pending;
+  const long long corner_chunk = nd > 0 ? nt : -1;
+  if (streamed) {
+    if (corner_chunk >= 0) cudaStreamWaitEvent(s, h->ev_chunk[corner_chunk], 0);
+  } else {
+    status_init_kernel<<<1, 1, 0, s>>>(h->d_status);
+    h->kernels_issued += 1;
+  }
+  // The first factorization after create launched directly finds A already
+  // ingested into MF by create's validation; a captured stage ingests on
+  // every replay.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusActive;
+  if (!h->mf_holds_a || cap != cudaStreamCaptureStatusNone) {
+    cudaMemsetAsync(h->d_MF, 0, sizeof(double) * h->mf_size, s);
+    launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, s);
+    h->kernels_issued += 1;
+    trace(h, "ingest");
+  }
+  h->mf_holds_a = false;
   double* corner = h->d_MF + mf_col_offset(sh, nt);
   for (long long i = 0; i < nt; ++i) {
     double* P = h->d_MF + mf_col_offset(sh, i);
     const long long lda = mf_lda(sh, i);
+    if (streamed) cudaStreamWaitEvent(s, h->ev_chunk[i], 0);
     if (i > 0) {
       const double* Pm = h->d_MF + mf_col_offset(sh, i - 1);
       const long long ldm = mf_lda(sh, i - 1);
@@ -532,7 +568,12 @@ void issue_factor(rgf_handle* h) {
         c.A = Cm; c.lda = ldm; c.B = Cm; c.ldb = ldm; c.transB = 1;
         c.C = c.D = corner; c.ldc = c.ldd = nd;
         c.alpha = -1.0; c.beta = 1.0; c.outLower = 1;
+        // With look-ahead, on the side stream, where C_{i-1} was computed
+        // (no fork needed): nothing else touches the corner until the last
+        // block's join, so the update leaves the critical path.
+        h->on_side = h->lookahead && h->side;
         gemm(h, c, SMALL);
+        h->on_side = false;
       }
     }
     panel_potrf(h, P, lda, (int)lda, (int)ns, (int)ns, (int)(i * ns));
@@ -817,6 +858,65 @@ void issue_solve(rgf_handle* h, int nrhs) {
   }
 }
 
+// ---- asynchronous upload ----
+// Queue the CSC on the upload stream in block-column chunks (the arrowhead
+// corner first, then block columns 0, 1, ... in factorization order): each
+// chunk's rows and values are copied, its MF panel cleared and its columns
+// ingested, then ev_chunk[i] is recorded.  Nothing waits here; the caller's
+// arrays are read until the first factorization (or finish_upload) returns,
+// as the reference reads them during factorize (RGF.H:87-89, 689-698).
+int start_upload(rgf_handle* h, const size_t* ia, const size_t* ja, const double* a) {
+  const BtaShape& sh = h->sh;
+  const long long nblk = sh.nt + (sh.nd > 0 ? 1 : 0);
+  RGF_CK(cudaStreamCreateWithFlags(&h->upload, cudaStreamNonBlocking));
+  h->ev_chunk.assign((size_t)nblk, nullptr);
+  for (auto& e : h->ev_chunk) RGF_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaStream_t u = h->upload;
+  // after what create queued on the main stream (workspace clears)
+  RGF_CK(cudaEventRecord(h->ev_fork, h->stream));
+  RGF_CK(cudaStreamWaitEvent(u, h->ev_fork, 0));
+  status_init_kernel<<<1, 1, 0, u>>>(h->d_status);
+  RGF_CK(cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (sh.n + 1), cudaMemcpyHostToDevice, u));
+  h->upload_pending = true;  // from here on release() waits for the stream
+  for (long long q = 0; q < nblk; ++q) {
+    const long long i = sh.nd > 0 ? (q == 0 ? sh.nt : q - 1) : q;
+    const long long c0 = i * sh.ns, c1 = i < sh.nt ? c0 + sh.ns : sh.n;
+    const size_t e0 = ia[c0], e1 = ia[c1];
+    if (e1 > e0) {
+      RGF_CK(cudaMemcpyAsync(h->d_ja + e0, ja + e0, sizeof(size_t) * (e1 - e0),
+                             cudaMemcpyHostToDevice, u));
+      RGF_CK(cudaMemcpyAsync(h->d_a + e0, a + e0, sizeof(double) * (e1 - e0),
+                             cudaMemcpyHostToDevice, u));
+    }
+    const long long o0 = mf_col_offset(sh, i);
+    const long long o1 = i < sh.nt ? mf_col_offset(sh, i + 1) : h->mf_size;
+    RGF_CK(cudaMemsetAsync(h->d_MF + o0, 0, sizeof(double) * (o1 - o0), u));
+    launch_ingest(sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, u, c0, c1);
+    RGF_CK(cudaGetLastError());
+    RGF_CK(cudaEventRecord(h->ev_chunk[(size_t)i], u));
+  }
+  h->mf_holds_a = true;
+  return RGF_OK;
+}
+
+// Wait (on the host) until the asynchronous upload is complete; afterwards
+// nothing reads the caller's arrays.  With check, a pattern error that the
+// ingests recorded is reported now, as a synchronous create would have.
+int finish_upload(rgf_handle* h, bool check) {
+  if (!h->upload_pending) return RGF_OK;
+  h->upload_pending = false;
+  RGF_CK(cudaStreamSynchronize(h->upload));
+  RGF_CK(cudaGetLastError());
+  if (!check) return RGF_OK;
+  DevStatus st;
+  RGF_CK(cudaMemcpy(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st.bad_input) {
+    h->mf_holds_a = false;  // the next factorization ingests (and reports) again
+    return RGF_EINVAL;
+  }
+  return RGF_OK;
+}
+
 // ---- graph capture / replay ----
 // The first run of a stage launches its kernels directly; from the second run
 // on, the stage is captured once into a CUDA graph and replayed.  A handle
@@ -825,7 +925,11 @@ void issue_solve(rgf_handle* h, int nrhs) {
 // the stage runs launch by launch.
 template <class F>
 int run_stage(rgf_handle* h, cudaGraphExec_t* exec, long long* nk, int* runs, F issue) {
-  if (h->timer_on || !h->trace_path.empty() || !h->opts.use_graphs || (!*exec && (*runs)++ == 0)) {
+  const bool direct =
+      h->timer_on || !h->trace_path.empty() || !h->opts.use_graphs || (!*exec && (*runs)++ == 0);
+  // a run that waits for an asynchronous upload is launched directly (its
+  // waits are on events recorded outside any capture)
+  if (direct || h->upload_pending) {
     h->kernels_issued = 0;
     if (!h->trace_path.empty()) {
       if (!h->trace_t0) cudaEventCreate(&h->trace_t0);
@@ -905,7 +1009,12 @@ int sync_and_check(rgf_handle* h) {
 
 int ensure_factored(rgf_handle* h) {
   if (h->factored) return RGF_OK;
+  const bool streamed = h->upload_pending;
   int st = run_stage(h, &h->g_factor, &h->k_factor, &h->runs_factor, [&] { issue_factor(h); });
+  if (streamed) {  // the stage waited for every block column; the copies are done too
+    const int su = finish_upload(h, false);
+    if (!st) st = su;
+  }
   if (st) return st;
   st = sync_and_check(h);
   if (st) return st;
@@ -967,7 +1076,11 @@ int validate_host_csc(const size_t* ia, long long n) {
 void release(rgf_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
+  // nothing may still use a buffer when it goes back to an arena (no
+  // implicit synchronization there, unlike cudaFree)
+  if (h->upload) cudaStreamSynchronize(h->upload);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->side) cudaStreamSynchronize(h->side);
   if (h->g_factor) cudaGraphExecDestroy(h->g_factor);
   if (h->g_selinv) cudaGraphExecDestroy(h->g_selinv);
   if (h->g_inv) cudaGraphExecDestroy(h->g_inv);
@@ -983,9 +1096,11 @@ void release(rgf_handle* h) {
                   h->d_res, h->d_gemm_ws, h->d_gemm_ws_side, h->d_ref, h->d_rhs2,
                   h->d_norms};
   for (void* p : bufs) dfree(p);
-  if (h->side) cudaStreamSynchronize(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  for (cudaEvent_t e : h->ev_chunk)
+    if (e) cudaEventDestroy(e);
+  if (h->upload) cudaStreamDestroy(h->upload);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1039,6 +1154,7 @@ int rgf_default_opts(rgf_opts* o) {
   o->device = -1;
   o->use_graphs = 1;
   o->fp64_diag = 1;
+  o->async_upload = 0;
   return RGF_OK;
 }
 
@@ -1058,6 +1174,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
   if (o.selinv_mode != RGF_SELINV_EXACT && o.selinv_mode != RGF_SELINV_COMPAT) return RGF_EINVAL;
   if (o.slices < 0 || o.slices > 8) return RGF_EINVAL;
   if (o.fp64_diag < 0 || o.fp64_diag > 2) return RGF_EINVAL;
+  if (o.async_upload < 0 || o.async_upload > 1) return RGF_EINVAL;
 
   int dev = o.device;
   if (dev < 0) {
@@ -1110,7 +1227,8 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     if ((st = dalloc(h, &h->d_gemm_ws_side, h->gemm_ws_elems))) break;
     // the CSC goes up in two halves on the two streams, so that two copy
     // engines move it at once; the main stream joins before anything reads it
-    {
+    // (asynchronous upload: below, in block-column chunks)
+    if (!o.async_upload) {
       const size_t h1 = (size_t)h->nnz / 2, h2 = (size_t)h->nnz - h1;
       if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice,
                           h->stream) ||
@@ -1136,11 +1254,16 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
       st = h->split_side->prepare((int)(ns + nd), (int)ns, 1, h->stream);
       if (st) break;
     }
+    if (o.async_upload) {  // copies and ingests overlap the first factorization
+      st = start_upload(h, ia, ja, a);
+      break;
+    }
     // validate the pattern once on the device
     status_init_kernel<<<1, 1, 0, h->stream>>>(h->d_status);
     cudaMemsetAsync(h->d_MF, 0, sizeof(double) * h->mf_size, h->stream);
     launch_ingest(h->sh, h->d_ia, h->d_ja, h->d_a, h->d_MF, h->d_status, h->stream);
     st = sync_and_check(h);
+    if (!st) h->mf_holds_a = true;
   } while (0);
   if (st) {
     release(h);
@@ -1161,7 +1284,11 @@ int rgf_create_hermitian(const size_t* ia, const size_t* ja, const double* a, si
   std::vector<double> a2;
   int st = hermitian_embed(ia, ja, a, ns, nt, nd, ia2, ja2, a2);
   if (st) return st;
-  st = rgf_create(ia2.data(), ja2.data(), a2.data(), 2 * ns, nt, 2 * nd, opts, out);
+  rgf_opts o;
+  rgf_default_opts(&o);
+  if (opts) o = *opts;
+  o.async_upload = 0;  // the embedding is freed on return: copy it now
+  st = rgf_create(ia2.data(), ja2.data(), a2.data(), 2 * ns, nt, 2 * nd, &o, out);
   if (st) return st;
   rgf_handle* h = *out;
   h->hermitian = true;
@@ -1292,6 +1419,8 @@ static int solve_real(rgf_handle* h, double* x, const double* b, size_t nrhs) {
   const bool refine = h->opts.precision == RGF_PREC_SPLIT;
   if (refine && !h->d_norms && (st = dalloc(h, &h->d_norms, 2 * 4096))) return st;
   if (refine && need * 3 > h->ref_cap) {
+    for (auto& kv : h->g_solve) cudaGraphExecDestroy(kv.second.first);  // they name d_ref
+    h->g_solve.clear();
     dfree(h->d_ref);
     h->device_bytes -= h->ref_cap * sizeof(double);
     h->ref_cap = 0;
@@ -1352,7 +1481,8 @@ int rgf_residual_norm(rgf_handle* h, const double* x, const double* b, double* n
   }
   if (cudaSetDevice(h->device) != cudaSuccess) return RGF_ECUDA;
   const long long n = h->sh.n;
-  int st;
+  int st = finish_upload(h, true);  // the product reads the device CSC
+  if (st) return st;
   if (!h->d_res && (st = dalloc(h, &h->d_res, 3 * n))) return st;
   RGF_CK(cudaMemcpyAsync(h->d_res, x, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
   RGF_CK(cudaMemcpyAsync(h->d_res + n, b, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
@@ -1615,10 +1745,14 @@ int rgf_batch_create(size_t count, const size_t* const* ia, const size_t* const*
   *out = nullptr;
   rgf_batch* b = new (std::nothrow) rgf_batch();
   if (!b) return RGF_ENOMEM;
+  rgf_opts o;
+  rgf_default_opts(&o);
+  if (opts) o = *opts;
+  o.async_upload = 0;  // a batch graph is captured over all instances: upload now
   int st = RGF_OK;
   for (size_t i = 0; i < count && !st; ++i) {
     rgf_handle* h = nullptr;
-    st = rgf_create(ia[i], ja[i], a[i], ns[i], nt[i], nd[i], opts, &h);
+    st = rgf_create(ia[i], ja[i], a[i], ns[i], nt[i], nd[i], &o, &h);
     if (!st) b->h.push_back(h);
   }
   if (!st) {

@@ -18,6 +18,39 @@ struct DevStatus {
   int pad;
 };
 
+// ---- programmatic dependent launch -------------------------------------------
+// Kernels are launched with programmatic stream serialization (launch_k): the
+// next kernel in a stream may be scheduled once every CTA of the running one
+// has called pdl_trigger() (placed after each kernel's main loop, so the next
+// kernel's CTAs become resident during the tail instead of after it), and
+// every kernel calls pdl_wait() before its first global memory access, which
+// returns once the previous kernel in the stream has completed and its writes
+// are visible.  Both are no-ops in a kernel launched without the attribute.
+// RGF_GB300_PDL=0 launches without it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  // not on the legacy default stream, which synchronizes with every stream
+  cfg.numAttrs = pdl_enabled() && s != nullptr && s != cudaStreamLegacy ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, args...);  // a failure stays the pending launch error
+}
+
 enum Tri { TRI_NONE = 0, TRI_LOWER = 1, TRI_UPPER = 2 };
 
 // D = alpha * op(A) * op(B) + beta * C, column-major, op(A) m x k, op(B) k x n.
@@ -117,8 +150,11 @@ long long mf_lda(const BtaShape& sh, long long i);
 long long mf_dense_row(const BtaShape& sh, long long i);
 
 // Scatter the device CSC into the (pre-zeroed) MF layout; one warp per column.
+// Columns [c_lo, c_hi) only (c_hi < 0: to the last column): every entry of a
+// column lands in its own block column's panel.
 void launch_ingest(const BtaShape& sh, const size_t* ia, const size_t* ja, const double* a,
-                   double* MF, DevStatus* st, cudaStream_t s);
+                   double* MF, DevStatus* st, cudaStream_t s, long long c_lo = 0,
+                   long long c_hi = -1);
 // Sum of nparts partial log sums, times 2, in a fixed order -> *out.
 // *out = 2 sum(log diag(L)) over the factor MF: per-block sums into parts
 // (logdet_parts(sh) of them), then a fixed-order total.

@@ -4,7 +4,11 @@
 // 64-bit integer fixed point before one conversion back to FP64.
 #pragma once
 
+#include <cuda.h>
+
 #include <cstddef>
+#include <map>
+#include <tuple>
 
 #include "rgf_internal.h"
 
@@ -46,6 +50,8 @@ class SplitEngine {
  private:
   SplitEngine() = default;
   int ensure_ws(size_t bytes);
+  bool map_for(CUtensorMap* out, void* base, int S, int Rp, int Kp);
+  std::map<std::tuple<void*, int, int, int>, CUtensorMap> maps_;
   int ensure_splitk(long long tiles, cudaStream_t s);
   int reserve(int max_rows, int max_k, int batch_hint);
   int slices_ = 0;

@@ -148,12 +148,31 @@ def test_not_spd_reports_column(rgf):
     assert s.info()["not_spd_column"] == col
 
 
-def test_pattern_violation_rejected(rgf):
+@pytest.mark.parametrize("async_upload", [False, True])
+def test_pattern_violation_rejected(rgf, async_upload):
     ns, nt, nd = 10, 4, 2
     ia, ja, a = gen.generate_bta(ns, nt, nd, 5)
     ja = ja.copy()
     # column 0 row entry moved into block 2 (outside the tridiagonal pattern)
     ja[int(ia[1]) - 1 - nd] = 2 * ns + 1
+    if not async_upload:  # validated before the constructor returns
+        with pytest.raises(rgf.RGFError) as e:
+            rgf.RGF(ia, ja, a, ns, nt, nd, async_upload=False)
+        assert e.value.status == 1
+        return
+    # asynchronous upload: the first call that factorizes reports it, and so
+    # does every later one (the pattern is ingested again)
+    s = rgf.RGF(ia, ja, a, ns, nt, nd)
+    for _ in range(2):
+        with pytest.raises(rgf.RGFError) as e:
+            s.factorize()
+        assert e.value.status == 1
+    s.close()
+    s = rgf.RGF(ia, ja, a, ns, nt, nd)  # residualNorm first: it waits for the upload
     with pytest.raises(rgf.RGFError) as e:
-        rgf.RGF(ia, ja, a, ns, nt, nd)
+        s.residualNorm(np.ones(s.n), np.ones(s.n))
     assert e.value.status == 1
+    with pytest.raises(rgf.RGFError) as e:
+        s.logDet()
+    assert e.value.status == 1
+    s.close()
