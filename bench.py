@@ -620,9 +620,17 @@ def run_rgf(args, w):
     ms_step = ms_total / args.steps
     value = replica_throughput(flops, ws, ms_step)
 
-    # end-to-end through the public API: host CSC -> device, diag -> host
+    # end-to-end through the public API: host CSC -> device, diag -> host, a
+    # new handle per step (as a caller that builds a solver per evaluation).
+    # The CSC upload is asynchronous (the Python default): it overlaps the
+    # first factorization.  The device-memory cache (rgf_set_device_cache)
+    # hands a destroyed handle's buffers to the next; the first iteration
+    # (untimed, reported as cold_ms) fills it.
     e2e_ms = []
     e2e_parts = None
+    e2e_cold = None
+    cache_bytes = 0 if args.no_device_cache else 64 << 30
+    rgf_gb300.set_device_cache(cache_bytes)
     for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -637,10 +645,14 @@ def run_rgf(args, w):
         h.close()
         t4 = time.perf_counter()
         dt = (t4 - t0) * 1e3
-        if i > 0:
+        if i == 0:
+            e2e_cold = dt
+        else:
             e2e_ms.append(dt)
-            e2e_parts = {"create_h2d_ms": (t1 - t0) * 1e3, "factorize_ms": (t2 - t1) * 1e3,
+            e2e_parts = {"create_ms": (t1 - t0) * 1e3,
+                         "factorize_with_h2d_ms": (t2 - t1) * 1e3,
                          "logdet_rgfdiag_d2h_ms": (t3 - t2) * 1e3, "destroy_ms": (t4 - t3) * 1e3}
+    rgf_gb300.set_device_cache(0)
     e2e_med = statistics.median(e2e_ms) if e2e_ms else float("nan")
     if dist and e2e_ms:
         e2e_med = max_over_ranks(max(e2e_ms), dist, "cuda")
@@ -778,7 +790,10 @@ def run_rgf(args, w):
                                h2d / 1e9, mf_bytes / 1e9)},
                 "e2e": ({"value": flops * ws / (e2e_med * 1e-3) / 1e12, "unit": "TFLOP/s",
                          "ms_per_step": e2e_med, "h2d_bytes_per_step": h2d,
-                         "d2h_bytes_per_step": d2h, "parts": e2e_parts} if e2e_ms else None),
+                         "d2h_bytes_per_step": d2h, "parts": e2e_parts,
+                         "upload": "asynchronous: the CSC copy overlaps the first factorization",
+                         "device_cache_bytes": cache_bytes,
+                         "cold_ms": e2e_cold} if e2e_ms else None),
                 "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": launches,
                 "stages": stages, "plain_fp64": plain, "split_native_fp64_diag": native_diag,
                 "solve": solve_info, "oracle_err": oracle_err,
@@ -825,6 +840,8 @@ def main():
     p.add_argument("--no-fp64-diag", action="store_true",
                    help="split precision: also run the diagonal blocks' inner updates as split products")
     p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--no-device-cache", action="store_true",
+                   help="e2e leg without the device-memory cache (every handle allocates)")
     p.add_argument("--ref-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-prefix", action="store_true",

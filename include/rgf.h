@@ -204,6 +204,18 @@ int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m,
  * stage graphs and its results. */
 int rgf_set_wait_limit(rgf_handle* h, int polls);
 
+/* Process-wide cache of device memory, off by default (max_bytes = 0).  With
+ * max_bytes > 0, the buffers of a destroyed handle (and of the library's other
+ * non-arena allocations) are kept, up to max_bytes in all, and handed to later
+ * allocations of exactly their size on their device: a process that creates
+ * and destroys handles of one shape in a loop (one per hyperparameter
+ * evaluation, say) then pays no cudaMalloc/cudaFree per handle.  The memory
+ * stays reserved for this library until a smaller limit (0 returns all of it)
+ * or until an allocation the driver cannot serve, which first returns the
+ * device's cached blocks.  rgf_device_cache_bytes reports the bytes held. */
+int rgf_set_device_cache(size_t max_bytes);
+int rgf_device_cache_bytes(size_t* held);
+
 /* Failure injection for tests, process-wide: the next `after` device
  * allocations of the library succeed, the one after that fails as if the
  * device were out of memory (the call returns RGF_ENOMEM), and later ones

@@ -144,6 +144,8 @@ _SIGS = {
     "rgf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
     "rgf_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
     "rgf_debug_fail_alloc_after": (C.c_int, [C.c_longlong]),
+    "rgf_set_device_cache": (C.c_int, [C.c_size_t]),
+    "rgf_device_cache_bytes": (C.c_int, [C.POINTER(C.c_size_t)]),
     "rgf_residual_norm_noalloc": (C.c_int, [C.c_size_t] + [C.c_void_p] * 7),
 }
 
@@ -192,6 +194,20 @@ def debug_fail_alloc_after(after: int) -> None:
     """Failure injection for tests: the next ``after`` device allocations of
     the library succeed and the one after fails (RGF_ENOMEM); -1 turns it off."""
     _check(load_library().rgf_debug_fail_alloc_after(int(after)), "rgf_debug_fail_alloc_after")
+
+
+def set_device_cache(max_bytes: int) -> None:
+    """Keep freed device buffers (up to ``max_bytes``) for later handles of the
+    same shape, so that create / destroy in a loop pay no cudaMalloc / cudaFree;
+    0 (the default) returns every cached buffer to the driver."""
+    _check(load_library().rgf_set_device_cache(int(max_bytes)), "rgf_set_device_cache")
+
+
+def device_cache_bytes() -> int:
+    """Bytes of device memory the cache holds (buffers not in use)."""
+    out = C.c_size_t()
+    _check(load_library().rgf_device_cache_bytes(C.byref(out)), "rgf_device_cache_bytes")
+    return out.value
 
 
 def measure_fp64_peak() -> float:

@@ -132,6 +132,7 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(GemmDesc g) {
       if (kt + TK < kr.khi) load(kt + TK);
 #pragma unroll
       for (int ks = 0; ks < TK; ks += 4) {
+        if (kt + ks >= kr.khi) break;  // a short last K tile: no products of the zero padding
         double af[F], bf[F];
 #pragma unroll
         for (int i = 0; i < F; ++i) af[i] = As[ks + (lane & 3)][wm + i * 8 + (lane >> 2)];

@@ -151,6 +151,29 @@ __global__ void copy_kernel(const double* X, long long ldx, double* Y, long long
   if (r < m && c < n) Y[r + (long long)c * ldy] = X[r + (long long)c * ldx];
 }
 
+// X(r, c) = X(c, r) for r < c: the strictly upper triangle of the n x n
+// matrix X (column-major, ld) from its lower one.  The CTA of source tile
+// (bi, bj), bi >= bj, reads that 32 x 32 lower tile along its columns into
+// shared memory and writes it transposed along the columns of tile (bj, bi);
+// no CTA reads a tile another one writes.
+__global__ void mirror_lower_kernel(double* X, long long ld, int n) {
+  __shared__ double t[32][33];  // t[column offset][row offset] of the source tile
+  pdl_wait();
+  pdl_trigger();
+  const int bi = blockIdx.x, bj = blockIdx.y;
+  if (bi < bj) return;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int k = ty; k < 32; k += 8) {
+    const int r = bi * 32 + tx, c = bj * 32 + k;
+    if (r < n && c < n) t[k][tx] = X[r + (long long)c * ld];
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int r = bj * 32 + tx, c = bi * 32 + k;  // X(r, c) = X(c, r) = t[tx][k]
+    if (r < c && c < n) X[r + (long long)c * ld] = t[tx][k];
+  }
+}
+
 // y = A x with A symmetric, stored as its lower CSC: column c contributes
 // a_rc x_c to y_r (scatter) and, off the diagonal, a_rc x_r to y_c (gather).
 // Entries outside the lower triangle (r < c) or past the last row (r >= n)
@@ -353,6 +376,12 @@ void launch_set_identity(double* X, long long ld, int m, int batch, long long st
   if (m <= 0 || batch <= 0) return;
   dim3 grid((m + 31) / 32, (m + 7) / 8, batch);
   launch_k(set_identity_kernel, grid, dim3(32, 8), 0, s, X, ld, m, stride);
+}
+
+void launch_mirror_lower(double* X, long long ld, int n, cudaStream_t s) {
+  if (n <= 1) return;
+  const unsigned nb = (unsigned)((n + 31) / 32);
+  launch_k(mirror_lower_kernel, dim3(nb, nb), dim3(32, 8), 0, s, X, ld, n);
 }
 
 void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,

@@ -262,6 +262,40 @@ bool pdl_enabled() {
   return on;
 }
 
+// Process-wide cache of freed device blocks (rgf_set_device_cache; off by
+// default).  A block freed outside an arena is kept, while the cache holds at
+// most `limit` bytes, for a later allocation of exactly its size on its
+// device -- a handle of the same shape gets its buffers back without a
+// cudaMalloc, and destroying one costs no cudaFree (whose unmapping of tens of
+// GB takes ~20 ms).  Blocks are freed only after the streams that used them
+// are synchronized (release(), the workspace resizes), so a cached block is
+// idle when it is handed out again.  An allocation that cudaMalloc cannot
+// serve returns the device's cached blocks to the driver and tries again.
+struct DeviceCache {
+  std::mutex mu;
+  size_t limit = 0, held = 0;
+  std::multimap<std::pair<int, size_t>, void*> free_blocks;  // (device, bytes) -> block
+  std::map<void*, std::pair<int, size_t>> sizes;             // live cudaMalloc blocks
+};
+static DeviceCache g_cache;
+
+static void cache_trim(size_t keep, int device) {  // g_cache.mu held
+  int cur = -1;
+  cudaGetDevice(&cur);
+  for (auto it = g_cache.free_blocks.begin();
+       it != g_cache.free_blocks.end() && g_cache.held > keep;) {
+    if (device >= 0 && it->first.first != device) {
+      ++it;
+      continue;
+    }
+    g_cache.held -= it->first.second;
+    cudaSetDevice(it->first.first);  // the block's own device
+    cudaFree(it->second);
+    it = g_cache.free_blocks.erase(it);
+  }
+  if (cur >= 0) cudaSetDevice(cur);
+}
+
 cudaError_t device_malloc(void** p, size_t bytes) {
   long long left = g_fail_alloc_after.load();
   while (left >= 0) {
@@ -277,11 +311,43 @@ cudaError_t device_malloc(void** p, size_t bytes) {
     *p = arena_alloc(t_arena, bytes);
     if (*p) return cudaSuccess;
   }
-  return cudaMalloc(p, bytes);
+  std::lock_guard<std::mutex> lk(g_cache.mu);
+  if (g_cache.limit == 0 && g_cache.held == 0) return cudaMalloc(p, bytes);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  auto it = g_cache.free_blocks.find({dev, bytes});
+  if (it != g_cache.free_blocks.end()) {
+    *p = it->second;
+    g_cache.held -= bytes;
+    g_cache.free_blocks.erase(it);
+  } else {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && g_cache.held > 0) {
+      cudaGetLastError();
+      cache_trim(0, dev);
+      e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  g_cache.sizes[*p] = {dev, bytes};
+  return cudaSuccess;
 }
 
 void device_free(void* p) {
   if (!p || arena_release(p)) return;
+  {
+    std::lock_guard<std::mutex> lk(g_cache.mu);
+    auto it = g_cache.sizes.find(p);
+    if (it != g_cache.sizes.end()) {
+      const std::pair<int, size_t> key = it->second;
+      g_cache.sizes.erase(it);
+      if (g_cache.held + key.second <= g_cache.limit) {
+        g_cache.free_blocks.emplace(key, p);
+        g_cache.held += key.second;
+        return;
+      }
+    }
+  }
   cudaFree(p);
 }
 }  // namespace rgf
@@ -743,10 +809,15 @@ void issue_selinv(rgf_handle* h) {
           h->kernels_issued++;
         }
       }
-      // Sigma_ii = L_ii^{-T} W = U_i (W^T)^T
+      // Sigma_ii = L_ii^{-T} W = U_i (W^T)^T, symmetric: only its lower
+      // triangle is computed (the output tiles above the diagonal, nearly
+      // half, are skipped), then mirrored
       GemmDesc g = mk(ins, ins, ins, Ui, ns, 0, h->d_T2, ns, 1, nullptr, 0, Q, lda, 1.0, 0.0);
       g.triA = TRI_UPPER;
+      g.outLower = 1;
       gemm(h, g, BULK);
+      launch_mirror_lower(Q, lda, ins, s);
+      h->kernels_issued++;
     } else {
       // the reference's recursion (RGF.H:444-502):
       // Sigma_ii = L^{-T} (I + B^T Sigma_{i+1,i+1} B + C^T Sigma_dd C) L^{-1}
@@ -1622,6 +1693,20 @@ int rgf_dgemm_device(int precision, int slices, char transa, char transb, int m,
   delete eng;
   cudaFree(st);
   return status;
+}
+
+int rgf_set_device_cache(size_t max_bytes) {
+  std::lock_guard<std::mutex> lk(rgf::g_cache.mu);
+  rgf::g_cache.limit = max_bytes;
+  rgf::cache_trim(max_bytes, -1);
+  return RGF_OK;
+}
+
+int rgf_device_cache_bytes(size_t* held) {
+  if (!held) return RGF_EINVAL;
+  std::lock_guard<std::mutex> lk(rgf::g_cache.mu);
+  *held = rgf::g_cache.held;
+  return RGF_OK;
 }
 
 int rgf_debug_fail_alloc_after(long long after) {

@@ -167,6 +167,8 @@ void launch_extract_diag(const BtaShape& sh, const double* MS, double* diag, cud
 void launch_set_identity(double* X, long long ld, int m, int batch, long long stride,
                          cudaStream_t s);
 // Y (m x n, ldy) = X (m x n, ldx); batched
+// Upper triangle of the symmetric n x n matrix X from its lower triangle.
+void launch_mirror_lower(double* X, long long ld, int n, cudaStream_t s);
 void launch_copy(const double* X, long long ldx, double* Y, long long ldy, int m, int n,
                  int batch, long long sX, long long sY, cudaStream_t s);
 // r = b - A x (symmetric, from the lower CSC) for the first column; then
