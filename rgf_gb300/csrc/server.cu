@@ -134,7 +134,11 @@ void run_request(rgf_server* s, Pending p) {
       st = r->ia ? RGF_ENOMEM : RGF_EINVAL;
     } else {
       rgf_handle* h = nullptr;
-      st = rgf_create(r->ia, r->ja, r->a, r->ns, r->nt, r->nd, &s->opts, &h);
+      // the request's arrays stay valid until it is done, so the CSC upload
+      // may overlap the factorization that follows at once
+      rgf_opts o = s->opts;
+      o.async_upload = 1;
+      st = rgf_create(r->ia, r->ja, r->a, r->ns, r->nt, r->nd, &o, &h);
       if (!st) st = rgf_factorize(h);
       if (!st) st = rgf_logdet(h, &r->logdet);
       std::lock_guard<std::mutex> lk(s->mu);
