@@ -134,11 +134,12 @@ void run_request(rgf_server* s, Pending p) {
       st = r->ia ? RGF_ENOMEM : RGF_EINVAL;
     } else {
       rgf_handle* h = nullptr;
-      // the request's arrays stay valid until it is done, so the CSC upload
-      // may overlap the factorization that follows at once
-      rgf_opts o = s->opts;
-      o.async_upload = 1;
-      st = rgf_create(r->ia, r->ja, r->a, r->ns, r->nt, r->nd, &o, &h);
+      // The server's opts decide the upload (synchronous by default).  The
+      // request's arrays stay valid until it is done, so async_upload is
+      // allowed, but it measured slower here: 8 slots of concurrent requests
+      // from pageable host arrays, ns up to 1500, served 17 req/s with the
+      // block-column chunked upload against 47 req/s with one copy each.
+      st = rgf_create(r->ia, r->ja, r->a, r->ns, r->nt, r->nd, &s->opts, &h);
       if (!st) st = rgf_factorize(h);
       if (!st) st = rgf_logdet(h, &r->logdet);
       std::lock_guard<std::mutex> lk(s->mu);
