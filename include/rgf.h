@@ -58,7 +58,10 @@ typedef struct rgf_opts {
                        units; 0 the bulk slice count                          */
   int async_upload; /* 1: rgf_create queues the CSC upload and returns; the
                        copies overlap the first factorization, which waits for
-                       each block column just before using it.  The caller's
+                       each block column just before using it.  Applies to
+                       page-locked arrays (cudaHostAlloc / cudaHostRegister);
+                       pageable ones are copied before rgf_create returns, as
+                       with 0 (the host stages such copies anyway).  The caller's
                        ia/ja/a must then stay valid and unchanged until the
                        first call that factorizes (rgf_factorize / rgf_logdet /
                        rgf_diag / rgf_solve) or rgf_residual_norm returns, or

@@ -249,7 +249,8 @@ class RGF:
 
     ``ia``/``ja`` are the column pointers and row indices (``size_t``) and
     ``a`` the values of the matrix's lower triangle in CSC form.  With
-    ``async_upload`` (the default) the copy to the device overlaps the first
+    ``async_upload`` (the default) and page-locked arrays (e.g. from
+    ``torch.Tensor.pin_memory``) the copy to the device overlaps the first
     factorization: the object keeps the arrays, as the reference keeps the
     pointers (RGF.H:87-89), and they must not be changed until the first
     factorize / logDet / RGFdiag / solve / residualNorm returns, which also

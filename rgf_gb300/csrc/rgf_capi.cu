@@ -1137,6 +1137,19 @@ int ensure_inverses(rgf_handle* h) {
   return RGF_OK;
 }
 
+// Whether host memory is page-locked (cudaHostAlloc / cudaHostRegister), so
+// that an asynchronous copy from it returns at once; from pageable memory the
+// calling thread stages every copy itself, and a chunked upload only adds
+// copies (measured much slower under concurrent requests).
+bool page_locked(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 int validate_host_csc(const size_t* ia, long long n) {
   if (ia[0] != 0) return RGF_EINVAL;
   for (long long c = 0; c < n; ++c)
@@ -1257,6 +1270,8 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     return RGF_ECUDA;
   }
   if (cudaSetDevice(dev) != cudaSuccess) return RGF_ECUDA;
+  // the asynchronous upload needs page-locked arrays (else: copied now)
+  const bool async = o.async_upload && page_locked(ia) && page_locked(ja) && page_locked(a);
 
   rgf_handle* h = new (std::nothrow) rgf_handle();
   if (!h) return RGF_ENOMEM;
@@ -1304,7 +1319,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
     // the CSC goes up in two halves on the two streams, so that two copy
     // engines move it at once; the main stream joins before anything reads it
     // (asynchronous upload: below, in block-column chunks)
-    if (!o.async_upload) {
+    if (!async) {
       const size_t h1 = (size_t)h->nnz / 2, h2 = (size_t)h->nnz - h1;
       if (cudaMemcpyAsync(h->d_ia, ia, sizeof(size_t) * (n + 1), cudaMemcpyHostToDevice,
                           h->stream) ||
@@ -1330,7 +1345,7 @@ int rgf_create(const size_t* ia, const size_t* ja, const double* a, size_t ns, s
       st = h->split_side->prepare((int)(ns + nd), (int)ns, 1, h->stream);
       if (st) break;
     }
-    if (o.async_upload) {  // copies and ingests overlap the first factorization
+    if (async) {  // copies and ingests overlap the first factorization
       st = start_upload(h, ia, ja, a);
       break;
     }

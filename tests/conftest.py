@@ -1,6 +1,7 @@
 import os
 import sys
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -17,3 +18,19 @@ def rgf():
     import rgf_gb300
     rgf_gb300.load_library()
     return rgf_gb300
+
+
+@pytest.fixture(scope="session")
+def pinned():
+    """Page-locked copies of host arrays (what the asynchronous upload needs):
+    pinned(ia, ja, a) -> the same arrays in pinned memory, same dtypes."""
+    torch = pytest.importorskip("torch")
+
+    def pin(*arrays):
+        out = []
+        for x in arrays:
+            x = np.ascontiguousarray(x)
+            v = x.view(np.int64) if x.dtype == np.uint64 else x
+            out.append(torch.from_numpy(v).pin_memory().numpy().view(x.dtype))
+        return tuple(out)
+    return pin
