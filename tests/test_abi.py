@@ -125,3 +125,27 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for f in py._fields_:
             assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
+
+
+def test_opts_struct_layout_matches_the_header():
+    """rgf_default_opts writes exactly the 16 ints of rgf_opts (precision,
+    slices, selinv_mode, device, use_graphs, fp64_diag, async_upload, 9
+    reserved), which the ctypes mirror declares in the same order."""
+    import ctypes
+    import rgf_gb300
+    lib = rgf_gb300.load_library()
+    assert ctypes.sizeof(rgf_gb300._Opts) == 16 * 4
+    buf = (ctypes.c_ubyte * 128)(*([0xAB] * 128))
+    assert lib.rgf_default_opts(ctypes.cast(buf, ctypes.POINTER(rgf_gb300._Opts))) == 0
+    assert bytes(buf[64:]) == b"\xab" * 64  # nothing written past the struct
+    o = rgf_gb300._Opts.from_buffer_copy(bytes(buf[:64]))
+    assert (o.precision, o.slices, o.selinv_mode, o.device, o.use_graphs, o.fp64_diag,
+            o.async_upload) == (0, 0, 0, -1, 1, 1, 0)
+
+
+def test_device_cache_api_needs_no_device():
+    import rgf_gb300
+    rgf_gb300.set_device_cache(1 << 20)
+    assert rgf_gb300.device_cache_bytes() == 0  # nothing freed into it yet
+    rgf_gb300.set_device_cache(0)
+    assert rgf_gb300.device_cache_bytes() == 0
