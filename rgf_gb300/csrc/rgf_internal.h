@@ -46,8 +46,10 @@ inline void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  // not on the legacy default stream, which synchronizes with every stream
-  cfg.numAttrs = pdl_enabled() && s != nullptr && s != cudaStreamLegacy ? 1 : 0;
+  // created streams only: not the default streams (the legacy one synchronizes
+  // with every stream)
+  cfg.numAttrs =
+      pdl_enabled() && s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread ? 1 : 0;
   cudaLaunchKernelEx(&cfg, kern, args...);  // a failure stays the pending launch error
 }
 
